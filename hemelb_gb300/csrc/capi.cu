@@ -1,0 +1,947 @@
+// Host side of the C ABI: context, single-device site layout, launches.
+//
+// The layout builder replaces the reference's Domain construction
+// (Code/geometry/Domain.cc:69-505: ProcessReadSites, PopulateWithReadData,
+// InitialiseNeighbourLookup) for one GPU: non-empty 8^3 blocks are put in Morton
+// order (the octree leaf order of Code/geometry/LookupTree.h:23-41), every block
+// keeps all 512 slots so neighbours are found by arithmetic plus a 27-entry
+// neighbour-block table, and only sites next to a wall or iolet carry a record.
+// The reference's contiguous site numbering (collision type, then block, then
+// in-block order) is kept as a permutation for the FieldData-layout accessors.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/hemelb_gb300.h"
+#include "lb_device.cuh"
+#include "lb_launch.h"
+
+using namespace hlbg;
+
+namespace {
+constexpr double kPI = 3.14159265358979323846264338327950288;  // Code/constants.h:18
+constexpr int kMonitorGrid = 152 * 4;
+constexpr int64_t kStageSites = 1 << 22;
+constexpr int kStepBatch = 1024;
+
+const int HCX[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+const int HCY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+const int HCZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+const int HINV[19] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+
+uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+  uint64_t m = 0;
+  for (int k = 0; k < 16; ++k) {
+    m |= (uint64_t)((x >> k) & 1u) << (3 * k + 2);
+    m |= (uint64_t)((y >> k) & 1u) << (3 * k + 1);
+    m |= (uint64_t)((z >> k) & 1u) << (3 * k);
+  }
+  return m;
+}
+
+int collision_type(uint32_t wall, int8_t site_type) {
+  // SiteData::GetCollisionType (Code/geometry/SiteDataBare.cc:102-145) mapped to
+  // the range index of Domain::ProcessReadSites (Code/geometry/Domain.cc:188-207)
+  if (wall == 0) return site_type == HLBG_SITE_INLET ? 2 : (site_type == HLBG_SITE_OUTLET ? 3 : 0);
+  return site_type == HLBG_SITE_INLET ? 4 : (site_type == HLBG_SITE_OUTLET ? 5 : 1);
+}
+
+double dot3(const double* a, const double* b) {
+  double s = 0.0;
+  s = s + a[0] * b[0];
+  s = s + a[1] * b[1];
+  s = s + a[2] * b[2];
+  return s;
+}
+
+template <class F>
+void parallel_for(int64_t n, F&& f) {
+  int nt = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  if (n < 4096) nt = 1;
+  std::atomic<int64_t> next{0};
+  auto work = [&]() {
+    for (;;) {
+      int64_t c = next.fetch_add(1024);
+      if (c >= n) break;
+      int64_t e = std::min(n, c + 1024);
+      for (int64_t i = c; i < e; ++i) f(i);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work);
+  work();
+  for (auto& t : th) t.join();
+}
+}  // namespace
+
+struct hlbg_ctx {
+  std::string err;
+  hlbg_params params{};
+  int prec = 0;
+  size_t elem = 8;
+  int64_t nb = 0, nslot = 0, nsites = 0, nrec = 0;
+  int64_t type_count[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<int32_t> h_block_xyz;
+  std::vector<int32_t> h_ref2slot;
+  std::vector<hlbg_iolet> inlets, outlets;
+  double min_density = 1.0;
+  uint64_t t1 = 1;
+  int cur = 0;
+  void* f[2] = {nullptr, nullptr};
+  int32_t* d_block_nbr = nullptr;
+  int32_t* d_block_xyz = nullptr;
+  uint32_t* d_site_code = nullptr;
+  uint8_t* d_block_bulk = nullptr;
+  uint32_t* d_b_wall = nullptr;
+  uint32_t* d_b_iolet = nullptr;
+  int32_t* d_b_ioid = nullptr;
+  int8_t* d_b_type = nullptr;
+  float* d_b_cut = nullptr;
+  int32_t* d_ref2slot = nullptr;
+  int32_t* d_ps_slot = nullptr;
+  int8_t* d_ps_dir = nullptr;
+  float* d_ps_q = nullptr;
+  int64_t n_ps = 0;
+  // per-range post step uses records directly (host list built on demand)
+  std::vector<int32_t> h_ps_slot;
+  std::vector<int8_t> h_ps_dir;
+  std::vector<float> h_ps_q;
+  std::vector<int32_t> h_rec_slot;
+  IoletDev* d_iolets = nullptr;
+  int n_io = 0;
+  double* d_io_tab = nullptr;   // [kStepBatch][2][n_io]: rho, umax
+  double* h_io_tab = nullptr;   // pinned staging
+  cudaEvent_t io_copied = nullptr;
+  double* d_stage = nullptr;
+  double* d_stage_rho = nullptr;
+  double* d_stage_u = nullptr;
+  int32_t* d_list = nullptr;
+  int64_t list_cap = 0;
+  double* d_part = nullptr;  // monitor partials
+  unsigned long long* d_part_bad = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  size_t dev_bytes = 0;
+  float fp16_scale = 1024.f;
+  bool initialised = false;
+};
+
+namespace {
+
+int fail(hlbg_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, HLBG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dev_alloc(hlbg_ctx* ctx, T** p, size_t count) {
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, HLBG_ERR_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                        cudaGetErrorString(e));
+  }
+  ctx->dev_bytes += bytes;
+  return HLBG_OK;
+}
+
+template <class T>
+int upload(hlbg_ctx* ctx, T** p, const std::vector<T>& v) {
+  int rc = dev_alloc(ctx, p, v.size());
+  if (rc) return rc;
+  if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return HLBG_OK;
+}
+
+void fill_args(hlbg_ctx* ctx, StepArgs& a) {
+  std::memset(&a, 0, sizeof(a));
+  a.f_old = ctx->f[ctx->cur];
+  a.f_new = ctx->f[ctx->cur ^ 1];
+  a.stride = ctx->nslot;
+  a.nslot = ctx->nslot;
+  a.block_nbr = ctx->d_block_nbr;
+  a.site_code = ctx->d_site_code;
+  a.block_bulk = ctx->d_block_bulk;
+  a.b_wall = ctx->d_b_wall;
+  a.b_iolet = ctx->d_b_iolet;
+  a.b_ioid = ctx->d_b_ioid;
+  a.b_type = ctx->d_b_type;
+  a.b_cut = ctx->d_b_cut;
+  a.iolets = ctx->d_iolets;
+  a.n_in = (int32_t)ctx->inlets.size();
+  a.kernel = ctx->params.kernel;
+  a.wall = ctx->params.wall;
+  a.inlet_model = ctx->params.inlet;
+  a.outlet_model = ctx->params.outlet;
+  // LbmParameters::CalcDerivedParams (Code/lb/LbmParameters.h:34-39) and
+  // TRT::Collide's second relaxation time (Code/lb/kernels/TRT.h:167-172)
+  const double tau = ctx->params.tau;
+  a.omega = -1.0 / tau;
+  const double tau_minus = 0.5 + (3.0 / 16.0) / (tau - 0.5);
+  a.omega_minus = -1.0 / tau_minus;
+  a.omega_f = (float)a.omega;
+  a.omega_minus_f = (float)a.omega_minus;
+  a.fp16_scale = ctx->fp16_scale;
+  a.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+}
+
+double iolet_density(const hlbg_ctx* ctx, const hlbg_iolet& io, uint64_t t) {
+  // InOutLetCosine::GetDensity (Code/lb/iolets/InOutLetCosine.cc:26-43);
+  // velocity iolets report 1.0 (Code/lb/iolets/InOutLetVelocity.cc:23-26)
+  if (io.model != HLBG_IOLET_COSINE) return 1.0;
+  double w = 2.0 * kPI / io.period;
+  double target = io.density_mean + io.density_amp * std::cos(w * (double)t + io.phase);
+  if (t >= io.warmup_steps) return target;
+  double interp = ((double)t) / ((double)io.warmup_steps);
+  return interp * target + (1. - interp) * ctx->min_density;
+}
+
+double iolet_umax(const hlbg_iolet& io, uint64_t t) {
+  // peak speed of InOutLetParabolicVelocity::GetVelocity at time t
+  // (Code/lb/iolets/InOutLetParabolicVelocity.cc:35-40); the pulsatile model
+  // scales it by (1 - cos(2 pi t / T)) / 2 first
+  if (io.model == HLBG_IOLET_COSINE) return 0.0;
+  double max = io.max_speed;
+  if (io.model == HLBG_IOLET_PULSATILE)
+    max = max * (0.5 * (1.0 - std::cos(2.0 * kPI * (double)t / io.vel_period)));
+  if (t < io.warmup_steps) max *= (double)t / (double)io.warmup_steps;
+  return max;
+}
+
+int launch_collide(hlbg_ctx* ctx, StepArgs& a, cudaStream_t st) {
+  switch (ctx->prec) {
+    case 0: launch_stream_collide_0(a, ctx->d_block_xyz, st); break;
+    case 1: launch_stream_collide_1(a, ctx->d_block_xyz, st); break;
+    default: launch_stream_collide_2(a, ctx->d_block_xyz, st); break;
+  }
+  CK(cudaGetLastError());
+  return HLBG_OK;
+}
+
+int launch_post(hlbg_ctx* ctx, const PostArgs& p, cudaStream_t st) {
+  switch (ctx->prec) {
+    case 0: launch_post_step_0(p, st); break;
+    case 1: launch_post_step_1(p, st); break;
+    default: launch_post_step_2(p, st); break;
+  }
+  CK(cudaGetLastError());
+  return HLBG_OK;
+}
+
+// Fill the iolet table for steps [t1, t1 + n) and copy it to the device.
+int upload_iolet_table(hlbg_ctx* ctx, int n, cudaStream_t st) {
+  if (ctx->n_io == 0) return HLBG_OK;
+  CK(cudaEventSynchronize(ctx->io_copied));
+  for (int k = 0; k < n; ++k) {
+    uint64_t t1 = ctx->t1 + k;
+    double* row = ctx->h_io_tab + (size_t)k * 2 * ctx->n_io;
+    int j = 0;
+    for (auto* v : {&ctx->inlets, &ctx->outlets})
+      for (auto& io : *v) {
+        // Nash: BoundaryValues::GetBoundaryDensity uses the 0-indexed step
+        // (Code/lb/iolets/BoundaryValues.cc:162-165); Ladd: BoundaryValues::GetTimeStep
+        // returns the 1-indexed step as unsigned int (BoundaryValues.h:67-70)
+        row[j] = iolet_density(ctx, io, t1 - 1);
+        row[ctx->n_io + j] = iolet_umax(io, (uint64_t)(unsigned int)t1);
+        ++j;
+      }
+  }
+  CK(cudaMemcpyAsync(ctx->d_io_tab, ctx->h_io_tab, sizeof(double) * 2 * ctx->n_io * n,
+                     cudaMemcpyHostToDevice, st));
+  CK(cudaEventRecord(ctx->io_copied, st));
+  return HLBG_OK;
+}
+
+int ensure_list(hlbg_ctx* ctx, int64_t n) {
+  if (ctx->list_cap >= n) return HLBG_OK;
+  if (ctx->d_list) cudaFree(ctx->d_list);
+  ctx->d_list = nullptr;
+  ctx->list_cap = 0;
+  int rc = dev_alloc(ctx, &ctx->d_list, (size_t)n);
+  if (rc) return rc;
+  ctx->list_cap = n;
+  return HLBG_OK;
+}
+
+int ensure_stage(hlbg_ctx* ctx) {
+  if (ctx->d_stage) return HLBG_OK;
+  int rc = dev_alloc(ctx, &ctx->d_stage, (size_t)kStageSites * 19);
+  if (!rc) rc = dev_alloc(ctx, &ctx->d_stage_rho, (size_t)kStageSites);
+  if (!rc) rc = dev_alloc(ctx, &ctx->d_stage_u, (size_t)kStageSites * 3);
+  return rc;
+}
+
+void fill_gather(hlbg_ctx* ctx, GatherArgs& g) {
+  std::memset(&g, 0, sizeof(g));
+  g.stride = ctx->nslot;
+  g.ref2slot = ctx->d_ref2slot;
+  g.fp16_scale = ctx->fp16_scale;
+  g.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+}
+
+int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
+  const int64_t nb = g->n_blocks;
+  const int NX = g->blocks[0], NY = g->blocks[1], NZ = g->blocks[2];
+  if (nb <= 0 || NX <= 0 || NY <= 0 || NZ <= 0 || !g->block_coords || !g->fluid_mask)
+    return fail(ctx, HLBG_ERR_INVAL, "geometry has no blocks");
+  if ((int64_t)NX * NY * NZ > (1ll << 31)) return fail(ctx, HLBG_ERR_INVAL, "block grid too large");
+  if (nb * 512 >= (1ll << 31)) return fail(ctx, HLBG_ERR_INVAL, "more than 2^31 slots");
+  // blocks in Morton order
+  std::vector<std::pair<uint64_t, int64_t>> order((size_t)nb);
+  for (int64_t b = 0; b < nb; ++b) {
+    int32_t x = g->block_coords[3 * b], y = g->block_coords[3 * b + 1], z = g->block_coords[3 * b + 2];
+    if (x < 0 || y < 0 || z < 0 || x >= NX || y >= NY || z >= NZ)
+      return fail(ctx, HLBG_ERR_INVAL, "block coordinate outside the block grid");
+    order[b] = {morton3(x, y, z), b};
+  }
+  std::sort(order.begin(), order.end());
+  std::vector<int32_t> new_of_old((size_t)nb);
+  std::vector<int32_t> grid((size_t)NX * NY * NZ, -1);
+  ctx->h_block_xyz.resize((size_t)nb * 3);
+  std::vector<uint64_t> mask((size_t)nb * 8);
+  for (int64_t nbi = 0; nbi < nb; ++nbi) {
+    int64_t ob = order[nbi].second;
+    new_of_old[ob] = (int32_t)nbi;
+    int32_t x = g->block_coords[3 * ob], y = g->block_coords[3 * ob + 1], z = g->block_coords[3 * ob + 2];
+    size_t gi = ((size_t)x * NY + y) * NZ + z;
+    if (grid[gi] >= 0) return fail(ctx, HLBG_ERR_INVAL, "duplicate block coordinates");
+    grid[gi] = (int32_t)nbi;
+    ctx->h_block_xyz[3 * nbi] = x;
+    ctx->h_block_xyz[3 * nbi + 1] = y;
+    ctx->h_block_xyz[3 * nbi + 2] = z;
+    for (int w = 0; w < 8; ++w) mask[nbi * 8 + w] = g->fluid_mask[ob * 8 + w];
+  }
+  std::vector<int32_t> bnbr((size_t)nb * 27);
+  parallel_for(nb, [&](int64_t b) {
+    int32_t x = ctx->h_block_xyz[3 * b], y = ctx->h_block_xyz[3 * b + 1], z = ctx->h_block_xyz[3 * b + 2];
+    for (int dx = -1; dx <= 1; ++dx)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dz = -1; dz <= 1; ++dz) {
+          int xx = x + dx, yy = y + dy, zz = z + dz;
+          int32_t v = -1;
+          if (xx >= 0 && yy >= 0 && zz >= 0 && xx < NX && yy < NY && zz < NZ)
+            v = grid[((size_t)xx * NY + yy) * NZ + zz];
+          bnbr[b * 27 + (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)] = v;
+        }
+  });
+  const int64_t nslot = nb * 512;
+  auto fluid = [&](int64_t s) { return (mask[(s >> 9) * 8 + ((s & 511) >> 6)] >> (s & 63)) & 1ull; };
+  auto neighbour = [&](int64_t s, int d) -> int64_t {
+    int l = (int)(s & 511);
+    int x = (l >> 6) + HCX[d], y = ((l >> 3) & 7) + HCY[d], z = (l & 7) + HCZ[d];
+    int ox = x >> 3, oy = y >> 3, oz = z >> 3;
+    int32_t nbk = bnbr[(s >> 9) * 27 + (ox + 1) * 9 + (oy + 1) * 3 + (oz + 1)];
+    if (nbk < 0) return -1;
+    return (int64_t)nbk * 512 + (((x & 7) * 8 + (y & 7)) * 8 + (z & 7));
+  };
+  // records from the input (by new slot)
+  std::vector<int32_t> rec_of_slot((size_t)nslot, -1);
+  const int64_t nin = g->n_link_sites;
+  for (int64_t r = 0; r < nin; ++r) {
+    int64_t os = g->link_site[r];
+    if (os < 0 || os >= nslot) return fail(ctx, HLBG_ERR_INVAL, "link site outside the blocks");
+    int64_t s = (int64_t)new_of_old[os >> 9] * 512 + (os & 511);
+    if (!fluid(s)) return fail(ctx, HLBG_ERR_INVAL, "link record for a solid site");
+    if (rec_of_slot[s] >= 0) return fail(ctx, HLBG_ERR_INVAL, "duplicate link record");
+    rec_of_slot[s] = (int32_t)r;
+  }
+  // fluid sites that have a non-fluid neighbour but no record get an empty one
+  std::vector<uint8_t> needs((size_t)nslot, 0);
+  parallel_for(nb, [&](int64_t b) {
+    for (int l = 0; l < 512; ++l) {
+      int64_t s = b * 512 + l;
+      if (!fluid(s)) continue;
+      bool edge = false;
+      for (int d = 1; d < 19 && !edge; ++d) {
+        int64_t n = neighbour(s, d);
+        if (n < 0 || !fluid(n)) edge = true;
+      }
+      needs[s] = edge || rec_of_slot[s] >= 0;
+    }
+  });
+  std::vector<uint32_t> code((size_t)nslot, 0);
+  std::vector<uint32_t> rw, ri;
+  std::vector<int32_t> rid;
+  std::vector<int8_t> rtype, stype;
+  std::vector<float> rcut;
+  const bool want_cut = ctx->params.wall == HLBG_WALL_BFL;
+  if (want_cut && !g->cut_distance && nin > 0)
+    return fail(ctx, HLBG_ERR_INVAL, "BFL walls need cut distances");
+  std::vector<int8_t> site_ctype((size_t)nslot, -1);
+  for (int64_t s = 0; s < nslot; ++s) {
+    if (!fluid(s)) continue;
+    if (!needs[s]) {
+      code[s] = 1;
+      site_ctype[s] = 0;
+      continue;
+    }
+    int64_t r = (int64_t)rw.size();
+    code[s] = (uint32_t)(2 + r);
+    ctx->h_rec_slot.push_back((int32_t)s);
+    int32_t ir = rec_of_slot[s];
+    uint32_t wm = 0, im = 0;
+    int32_t io = -1;
+    int8_t st = HLBG_SITE_FLUID;
+    if (ir >= 0) {
+      wm = g->wall_mask[ir];
+      im = g->iolet_mask[ir];
+      io = g->iolet_id[ir];
+      st = g->site_type ? g->site_type[ir] : (int8_t)HLBG_SITE_FLUID;
+    }
+    int ct = collision_type(wm, st);
+    if (im && ct < 2) return fail(ctx, HLBG_ERR_INVAL, "iolet links on a site of fluid type");
+    if (ct >= 2 && im) {
+      bool inl = (ct == 2 || ct == 4);
+      int lim = (int)(inl ? ctx->inlets.size() : ctx->outlets.size());
+      if (io < 0 || io >= lim) return fail(ctx, HLBG_ERR_INVAL, "iolet id out of range");
+    }
+    rw.push_back(wm);
+    ri.push_back(im);
+    rid.push_back(io);
+    rtype.push_back((int8_t)ct);
+    site_ctype[s] = (int8_t)ct;
+    if (want_cut)
+      for (int k = 0; k < 18; ++k)
+        rcut.push_back(ir >= 0 && g->cut_distance ? g->cut_distance[ir * 18 + k] : -1.0f);
+  }
+  ctx->nrec = (int64_t)rw.size();
+  std::vector<uint8_t> bulk((size_t)nb, 0);
+  for (int64_t b = 0; b < nb; ++b) {
+    bool all = true;
+    for (int l = 0; l < 512 && all; ++l) all = code[b * 512 + l] == 1;
+    bulk[b] = all;
+  }
+  // contiguous site ids (Domain::PopulateWithReadData order)
+  int64_t cnt[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t s = 0; s < nslot; ++s)
+    if (site_ctype[s] >= 0) cnt[site_ctype[s]]++;
+  int64_t off[6];
+  off[0] = 0;
+  for (int t = 1; t < 6; ++t) off[t] = off[t - 1] + cnt[t - 1];
+  ctx->nsites = off[5] + cnt[5];
+  for (int t = 0; t < 6; ++t) ctx->type_count[t] = cnt[t];
+  ctx->h_ref2slot.assign((size_t)ctx->nsites, 0);
+  for (int64_t s = 0; s < nslot; ++s)
+    if (site_ctype[s] >= 0) ctx->h_ref2slot[off[site_ctype[s]]++] = (int32_t)s;
+  // BFL PostStep links
+  if (want_cut) {
+    for (int64_t r = 0; r < ctx->nrec; ++r) {
+      int ct = rtype[r];
+      if (!(ct == 1 || ct == 4 || ct == 5)) continue;
+      for (int d = 1; d < 19; ++d) {
+        if (!((rw[r] >> (d - 1)) & 1u)) continue;
+        int inv = HINV[d];
+        float q = rcut[r * 18 + d - 1];
+        if (((rw[r] >> (inv - 1)) & 1u) || !(q < 0.5f)) continue;
+        ctx->h_ps_slot.push_back(ctx->h_rec_slot[r]);
+        ctx->h_ps_dir.push_back((int8_t)d);
+        ctx->h_ps_q.push_back(q);
+      }
+    }
+  }
+  ctx->n_ps = (int64_t)ctx->h_ps_slot.size();
+  ctx->nb = nb;
+  ctx->nslot = nslot;
+  // device copies
+  int rc;
+  if ((rc = upload(ctx, &ctx->d_block_nbr, bnbr))) return rc;
+  if ((rc = upload(ctx, &ctx->d_block_xyz, ctx->h_block_xyz))) return rc;
+  if ((rc = upload(ctx, &ctx->d_site_code, code))) return rc;
+  if ((rc = upload(ctx, &ctx->d_block_bulk, bulk))) return rc;
+  if ((rc = upload(ctx, &ctx->d_b_wall, rw))) return rc;
+  if ((rc = upload(ctx, &ctx->d_b_iolet, ri))) return rc;
+  if ((rc = upload(ctx, &ctx->d_b_ioid, rid))) return rc;
+  if ((rc = upload(ctx, &ctx->d_b_type, rtype))) return rc;
+  if (want_cut && (rc = upload(ctx, &ctx->d_b_cut, rcut))) return rc;
+  if ((rc = upload(ctx, &ctx->d_ref2slot, ctx->h_ref2slot))) return rc;
+  if ((rc = upload(ctx, &ctx->d_ps_slot, ctx->h_ps_slot))) return rc;
+  if ((rc = upload(ctx, &ctx->d_ps_dir, ctx->h_ps_dir))) return rc;
+  if ((rc = upload(ctx, &ctx->d_ps_q, ctx->h_ps_q))) return rc;
+  return HLBG_OK;
+}
+
+int run_post(hlbg_ctx* ctx, cudaStream_t st, const int32_t* slot, const int8_t* dir, const float* q,
+             int64_t count) {
+  if (ctx->params.wall != HLBG_WALL_BFL || count == 0) return HLBG_OK;
+  PostArgs p{};
+  p.f_new = ctx->f[ctx->cur ^ 1];
+  p.stride = ctx->nslot;
+  p.slot = slot;
+  p.dir = dir;
+  p.q = q;
+  p.count = count;
+  p.fp16_scale = ctx->fp16_scale;
+  p.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+  return launch_post(ctx, p, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hlbg_version(void) { return "hemelb_gb300 0.1 (sm_103a, D3Q19)"; }
+
+const char* hlbg_last_error(const hlbg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void hlbg_destroy(hlbg_ctx* ctx) {
+  if (!ctx) return;
+  void* ptrs[] = {ctx->f[0],        ctx->f[1],        ctx->d_block_nbr, ctx->d_block_xyz,
+                  ctx->d_site_code, ctx->d_block_bulk, ctx->d_b_wall,   ctx->d_b_iolet,
+                  ctx->d_b_ioid,    ctx->d_b_type,    ctx->d_b_cut,     ctx->d_ref2slot,
+                  ctx->d_ps_slot,   ctx->d_ps_dir,    ctx->d_ps_q,      ctx->d_iolets,
+                  ctx->d_io_tab,    ctx->d_stage,     ctx->d_stage_rho, ctx->d_stage_u,
+                  ctx->d_list,      ctx->d_part,      ctx->d_part_bad};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->h_io_tab) cudaFreeHost(ctx->h_io_tab);
+  if (ctx->io_copied) cudaEventDestroy(ctx->io_copied);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int hlbg_create(const hlbg_geometry* g, const hlbg_params* p, const hlbg_iolet* inlets,
+                int32_t n_inlets, const hlbg_iolet* outlets, int32_t n_outlets, hlbg_ctx** out) {
+  if (!out) return HLBG_ERR_INVAL;
+  *out = nullptr;
+  if (!g || !p) return HLBG_ERR_INVAL;
+  hlbg_ctx* ctx = new (std::nothrow) hlbg_ctx();
+  if (!ctx) return HLBG_ERR_OOM;
+  *out = ctx;  // returned even on failure so hlbg_last_error can explain; caller destroys
+  if (g->q != 19) return fail(ctx, HLBG_ERR_INVAL, "the device path implements D3Q19 only");
+  if (g->block_size != 8) return fail(ctx, HLBG_ERR_INVAL, "block_size must be 8");
+  if (p->kernel != HLBG_KERNEL_LBGK && p->kernel != HLBG_KERNEL_TRT)
+    return fail(ctx, HLBG_ERR_INVAL, "unknown kernel");
+  if (p->wall != HLBG_WALL_SBB && p->wall != HLBG_WALL_BFL) return fail(ctx, HLBG_ERR_INVAL, "unknown wall");
+  if ((p->inlet != HLBG_IOLET_NASH && p->inlet != HLBG_IOLET_LADD) ||
+      (p->outlet != HLBG_IOLET_NASH && p->outlet != HLBG_IOLET_LADD))
+    return fail(ctx, HLBG_ERR_INVAL, "unknown iolet streamer");
+  if (p->precision < HLBG_FP64 || p->precision > HLBG_FP16)
+    return fail(ctx, HLBG_ERR_INVAL, "unknown precision");
+  if (!(p->tau > 0.5)) return fail(ctx, HLBG_ERR_INVAL, "tau must exceed 0.5");
+  if (n_inlets < 0 || n_outlets < 0 || (n_inlets && !inlets) || (n_outlets && !outlets))
+    return fail(ctx, HLBG_ERR_INVAL, "bad iolet arrays");
+  ctx->params = *p;
+  ctx->prec = p->precision;
+  ctx->elem = p->precision == HLBG_FP64 ? 8 : (p->precision == HLBG_FP32DEV ? 4 : 2);
+  ctx->inlets.assign(inlets, inlets + n_inlets);
+  ctx->outlets.assign(outlets, outlets + n_outlets);
+  // iolet models must match the streamer: Nash reads a density, Ladd a velocity
+  for (auto& io : ctx->inlets)
+    if ((p->inlet == HLBG_IOLET_NASH) != (io.model == HLBG_IOLET_COSINE))
+      return fail(ctx, HLBG_ERR_INVAL, "inlet model does not match the inlet streamer");
+  for (auto& io : ctx->outlets)
+    if ((p->outlet == HLBG_IOLET_NASH) != (io.model == HLBG_IOLET_COSINE))
+      return fail(ctx, HLBG_ERR_INVAL, "outlet model does not match the outlet streamer");
+  // LBM::PrepareBoundaryObjects (Code/lb/lb.hpp:127-152)
+  double mind = 1.7976931348623157e308;
+  for (auto* v : {&ctx->inlets, &ctx->outlets})
+    for (auto& io : *v) {
+      double dm = io.model == HLBG_IOLET_COSINE ? io.density_mean - io.density_amp : 1.0;
+      mind = std::min(mind, dm);
+    }
+  ctx->min_density = mind;
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&ctx->ev0));
+  CK(cudaEventCreate(&ctx->ev1));
+  CK(cudaEventCreateWithFlags(&ctx->io_copied, cudaEventDisableTiming));
+  CK(cudaEventRecord(ctx->io_copied, ctx->stream));
+  int rc = build_layout(ctx, g);
+  if (rc) return rc;
+  // iolet constants
+  ctx->n_io = (int)(ctx->inlets.size() + ctx->outlets.size());
+  std::vector<IoletDev> iod;
+  for (auto* v : {&ctx->inlets, &ctx->outlets})
+    for (auto& io : *v) {
+      IoletDev d{};
+      double mag = std::sqrt(dot3(io.normal, io.normal));  // InOutLet::SetNormal
+      for (int k = 0; k < 3; ++k) {
+        d.pos[k] = io.position[k];
+        d.n[k] = io.normal[k] / mag;
+        d.nf[k] = (double)(float)d.n[k];
+      }
+      d.radius = io.radius;
+      d.model = io.model;
+      iod.push_back(d);
+    }
+  if ((rc = upload(ctx, &ctx->d_iolets, iod))) return rc;
+  if (ctx->n_io) {
+    if ((rc = dev_alloc(ctx, &ctx->d_io_tab, (size_t)kStepBatch * 2 * ctx->n_io))) return rc;
+    CK(cudaMallocHost((void**)&ctx->h_io_tab, sizeof(double) * kStepBatch * 2 * ctx->n_io));
+  }
+  // distributions
+  for (int k = 0; k < 2; ++k) {
+    size_t bytes = (size_t)19 * ctx->nslot * ctx->elem;
+    cudaError_t e = cudaMalloc(&ctx->f[k], bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, HLBG_ERR_OOM, "distribution arrays: " + std::string(cudaGetErrorString(e)));
+    }
+    ctx->dev_bytes += bytes;
+    CK(cudaMemsetAsync(ctx->f[k], 0, bytes, ctx->stream));
+  }
+  if ((rc = dev_alloc(ctx, &ctx->d_part, (size_t)kMonitorGrid * 3))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->d_part_bad, (size_t)kMonitorGrid))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return HLBG_OK;
+}
+
+int64_t hlbg_site_count(const hlbg_ctx* ctx) { return ctx ? ctx->nsites : 0; }
+int64_t hlbg_slot_count(const hlbg_ctx* ctx) { return ctx ? ctx->nslot : 0; }
+size_t hlbg_device_bytes(const hlbg_ctx* ctx) { return ctx ? ctx->dev_bytes : 0; }
+
+int hlbg_collision_counts(const hlbg_ctx* ctx, int64_t counts[6]) {
+  if (!ctx || !counts) return HLBG_ERR_INVAL;
+  for (int t = 0; t < 6; ++t) counts[t] = ctx->type_count[t];
+  return HLBG_OK;
+}
+
+int hlbg_site_order(const hlbg_ctx* ctx, int64_t* ref_to_slot) {
+  if (!ctx || !ref_to_slot) return HLBG_ERR_INVAL;
+  for (int64_t i = 0; i < ctx->nsites; ++i) ref_to_slot[i] = ctx->h_ref2slot[i];
+  return HLBG_OK;
+}
+
+int hlbg_init_equilibrium(hlbg_ctx* ctx, double density, double vx, double vy, double vz) {
+  if (!ctx) return HLBG_ERR_INVAL;
+  if (!(density > 0.0)) return fail(ctx, HLBG_ERR_INVAL, "density must be positive");
+  // EquilibriumInitialCondition::SetFs (Code/lb/InitialCondition.hpp:40-52):
+  // feq(rho, rho*u) with Lattice::CalculateFeq's scalar order, for every site
+  InitArgs ia{};
+  ia.f0 = ctx->f[0];
+  ia.f1 = ctx->f[1];
+  ia.stride = ctx->nslot;
+  ia.nslot = ctx->nslot;
+  ia.site_code = ctx->d_site_code;
+  ia.block_bulk = ctx->d_block_bulk;
+  ia.fp16_scale = ctx->fp16_scale;
+  ia.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+  const double mx = density * vx, my = density * vy, mz = density * vz;
+  const double density_1 = 1. / density;
+  const double m2 = mx * mx + my * my + mz * mz;
+  for (int i = 0; i < 19; ++i) {
+    const double mde = HCX[i] * mx + HCY[i] * my + HCZ[i] * mz;
+    const double w = weight_d(i);
+    const double feq = w * (density - (3. / 2.) * m2 * density_1 + (9. / 2.) * density_1 * mde * mde +
+                            3. * mde);
+    ia.value[i] = ctx->prec == 0 ? feq : feq - w;
+  }
+  switch (ctx->prec) {
+    case 0: launch_init_uniform_0(ia, ctx->stream); break;
+    case 1: launch_init_uniform_1(ia, ctx->stream); break;
+    default: launch_init_uniform_2(ia, ctx->stream); break;
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->cur = 0;
+  ctx->t1 = 1;
+  ctx->initialised = true;
+  return HLBG_OK;
+}
+
+int hlbg_init_equilibrium_field(hlbg_ctx* ctx, const double* rho, const double* u) {
+  if (!ctx || !rho || !u) return HLBG_ERR_INVAL;
+  int rc = ensure_stage(ctx);
+  if (rc) return rc;
+  for (int64_t first = 0; first < ctx->nsites; first += kStageSites) {
+    int64_t n = std::min<int64_t>(kStageSites, ctx->nsites - first);
+    CK(cudaMemcpyAsync(ctx->d_stage_rho, rho + first, sizeof(double) * n, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_stage_u, u + 3 * first, sizeof(double) * 3 * n, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    FieldArgs fa{};
+    fa.f0 = ctx->f[0];
+    fa.f1 = ctx->f[1];
+    fa.stride = ctx->nslot;
+    fa.ref2slot = ctx->d_ref2slot;
+    fa.first = first;
+    fa.count = n;
+    fa.rho = ctx->d_stage_rho;
+    fa.u = ctx->d_stage_u;
+    fa.fp16_scale = ctx->fp16_scale;
+    fa.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+    switch (ctx->prec) {
+      case 0: launch_init_field_0(fa, ctx->stream); break;
+      case 1: launch_init_field_1(fa, ctx->stream); break;
+      default: launch_init_field_2(fa, ctx->stream); break;
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  ctx->cur = 0;
+  ctx->t1 = 1;
+  ctx->initialised = true;
+  return HLBG_OK;
+}
+
+int hlbg_step(hlbg_ctx* ctx, int32_t nsteps, void* cuda_stream) {
+  if (!ctx || nsteps < 0) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
+  StepArgs a;
+  for (int done = 0; done < nsteps;) {
+    int n = std::min(kStepBatch, nsteps - done);
+    int rc = upload_iolet_table(ctx, n, st);
+    if (rc) return rc;
+    for (int k = 0; k < n; ++k) {
+      fill_args(ctx, a);
+      a.iolet_rho = ctx->d_io_tab + (size_t)k * 2 * ctx->n_io;
+      a.iolet_umax = a.iolet_rho + ctx->n_io;
+      if ((rc = launch_collide(ctx, a, st))) return rc;
+      if ((rc = run_post(ctx, st, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps))) return rc;
+      ctx->cur ^= 1;  // FieldData::SwapOldAndNew
+      ctx->t1++;      // SimulationState::Increment
+    }
+    done += n;
+  }
+  return HLBG_OK;
+}
+
+int hlbg_sync(hlbg_ctx* ctx) {
+  if (!ctx) return HLBG_ERR_INVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return HLBG_OK;
+}
+
+int hlbg_stream_and_collide_range(hlbg_ctx* ctx, int64_t first, int64_t count) {
+  if (!ctx || first < 0 || count < 0 || first + count > ctx->nsites) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  if (count == 0) return HLBG_OK;
+  int rc = ensure_list(ctx, count);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ctx->d_list, ctx->d_ref2slot + first, sizeof(int32_t) * count,
+                     cudaMemcpyDeviceToDevice, ctx->stream));
+  if ((rc = upload_iolet_table(ctx, 1, ctx->stream))) return rc;
+  StepArgs a;
+  fill_args(ctx, a);
+  a.iolet_rho = ctx->d_io_tab;
+  a.iolet_umax = ctx->d_io_tab + ctx->n_io;
+  a.list = ctx->d_list;
+  a.list_count = count;
+  if ((rc = launch_collide(ctx, a, ctx->stream))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return HLBG_OK;
+}
+
+int hlbg_post_step_range(hlbg_ctx* ctx, int64_t first, int64_t count) {
+  if (!ctx || first < 0 || count < 0 || first + count > ctx->nsites) return HLBG_ERR_INVAL;
+  if (ctx->params.wall != HLBG_WALL_BFL || count == 0 || ctx->n_ps == 0) return HLBG_OK;
+  // the PostStep links whose site lies in the contiguous-id range
+  std::vector<uint8_t> in((size_t)ctx->nslot, 0);
+  for (int64_t i = first; i < first + count; ++i) in[ctx->h_ref2slot[i]] = 1;
+  std::vector<int32_t> sl;
+  std::vector<int8_t> dr;
+  std::vector<float> qq;
+  for (int64_t k = 0; k < ctx->n_ps; ++k)
+    if (in[ctx->h_ps_slot[k]]) {
+      sl.push_back(ctx->h_ps_slot[k]);
+      dr.push_back(ctx->h_ps_dir[k]);
+      qq.push_back(ctx->h_ps_q[k]);
+    }
+  if (sl.empty()) return HLBG_OK;
+  int32_t* ds = nullptr;
+  int8_t* dd = nullptr;
+  float* dq = nullptr;
+  int rc = HLBG_OK;
+  if (!rc) rc = upload(ctx, &ds, sl);
+  if (!rc) rc = upload(ctx, &dd, dr);
+  if (!rc) rc = upload(ctx, &dq, qq);
+  if (!rc) rc = run_post(ctx, ctx->stream, ds, dd, dq, (int64_t)sl.size());
+  cudaStreamSynchronize(ctx->stream);
+  size_t freed = sl.size() * (sizeof(int32_t) + sizeof(int8_t) + sizeof(float));
+  if (ds) cudaFree(ds);
+  if (dd) cudaFree(dd);
+  if (dq) cudaFree(dq);
+  ctx->dev_bytes -= std::min(ctx->dev_bytes, freed);
+  return rc;
+}
+
+int hlbg_swap(hlbg_ctx* ctx) {
+  if (!ctx) return HLBG_ERR_INVAL;
+  ctx->cur ^= 1;
+  ctx->t1++;
+  return HLBG_OK;
+}
+
+static int gather_common(hlbg_ctx* ctx, double* out, int32_t which, bool to_host) {
+  if (!ctx || !out || (which != 0 && which != 1)) return HLBG_ERR_INVAL;
+  int rc = ensure_stage(ctx);
+  if (rc) return rc;
+  GatherArgs ga;
+  fill_gather(ctx, ga);
+  ga.f = ctx->f[ctx->cur ^ which];
+  for (int64_t first = 0; first < ctx->nsites; first += kStageSites) {
+    int64_t n = std::min<int64_t>(kStageSites, ctx->nsites - first);
+    ga.first = first;
+    ga.count = n;
+    ga.aos = to_host ? ctx->d_stage : out + first * 19;
+    switch (ctx->prec) {
+      case 0: launch_gather_0(ga, ctx->stream); break;
+      case 1: launch_gather_1(ga, ctx->stream); break;
+      default: launch_gather_2(ga, ctx->stream); break;
+    }
+    CK(cudaGetLastError());
+    if (to_host) {
+      CK(cudaMemcpyAsync(out + first * 19, ctx->d_stage, sizeof(double) * 19 * n,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return HLBG_OK;
+}
+
+static int scatter_common(hlbg_ctx* ctx, const double* in, int32_t which, bool from_host) {
+  if (!ctx || !in || (which != 0 && which != 1)) return HLBG_ERR_INVAL;
+  int rc = ensure_stage(ctx);
+  if (rc) return rc;
+  GatherArgs ga;
+  fill_gather(ctx, ga);
+  ga.f_out = ctx->f[ctx->cur ^ which];
+  for (int64_t first = 0; first < ctx->nsites; first += kStageSites) {
+    int64_t n = std::min<int64_t>(kStageSites, ctx->nsites - first);
+    ga.first = first;
+    ga.count = n;
+    if (from_host) {
+      CK(cudaMemcpyAsync(ctx->d_stage, in + first * 19, sizeof(double) * 19 * n,
+                         cudaMemcpyHostToDevice, ctx->stream));
+      ga.aos = ctx->d_stage;
+    } else {
+      ga.aos = const_cast<double*>(in) + first * 19;
+    }
+    switch (ctx->prec) {
+      case 0: launch_scatter_0(ga, ctx->stream); break;
+      case 1: launch_scatter_1(ga, ctx->stream); break;
+      default: launch_scatter_2(ga, ctx->stream); break;
+    }
+    CK(cudaGetLastError());
+    if (from_host) CK(cudaStreamSynchronize(ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->initialised = true;
+  return HLBG_OK;
+}
+
+int hlbg_get_f(hlbg_ctx* ctx, double* host, int32_t which) { return gather_common(ctx, host, which, true); }
+int hlbg_put_f(hlbg_ctx* ctx, const double* host, int32_t which) {
+  return scatter_common(ctx, host, which, true);
+}
+int hlbg_get_f_device(hlbg_ctx* ctx, double* dev, int32_t which) {
+  return gather_common(ctx, dev, which, false);
+}
+int hlbg_put_f_device(hlbg_ctx* ctx, const double* dev, int32_t which) {
+  return scatter_common(ctx, dev, which, false);
+}
+
+int hlbg_get_macro(hlbg_ctx* ctx, double* rho, double* u) {
+  if (!ctx || !rho || !u) return HLBG_ERR_INVAL;
+  int rc = ensure_stage(ctx);
+  if (rc) return rc;
+  GatherArgs ga;
+  fill_gather(ctx, ga);
+  ga.f = ctx->f[ctx->cur];
+  for (int64_t first = 0; first < ctx->nsites; first += kStageSites) {
+    int64_t n = std::min<int64_t>(kStageSites, ctx->nsites - first);
+    ga.first = first;
+    ga.count = n;
+    ga.rho = ctx->d_stage_rho;
+    ga.u = ctx->d_stage_u;
+    switch (ctx->prec) {
+      case 0: launch_macro_0(ga, ctx->stream); break;
+      case 1: launch_macro_1(ga, ctx->stream); break;
+      default: launch_macro_2(ga, ctx->stream); break;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rho + first, ctx->d_stage_rho, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(u + 3 * first, ctx->d_stage_u, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return HLBG_OK;
+}
+
+int hlbg_reduce(hlbg_ctx* ctx, hlbg_stats* out) {
+  if (!ctx || !out) return HLBG_ERR_INVAL;
+  MonitorArgs ma{};
+  ma.f_cur = ctx->f[ctx->cur];
+  ma.f_prev = ctx->f[ctx->cur ^ 1];
+  ma.stride = ctx->nslot;
+  ma.nslot = ctx->nslot;
+  ma.site_code = ctx->d_site_code;
+  ma.block_bulk = ctx->d_block_bulk;
+  ma.part_mass = ctx->d_part;
+  ma.part_max = ctx->d_part + kMonitorGrid;
+  ma.part_min = ctx->d_part + 2 * kMonitorGrid;
+  ma.part_bad = ctx->d_part_bad;
+  ma.fp16_scale = ctx->fp16_scale;
+  ma.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+  switch (ctx->prec) {
+    case 0: launch_monitor_0(ma, kMonitorGrid, ctx->stream); break;
+    case 1: launch_monitor_1(ma, kMonitorGrid, ctx->stream); break;
+    default: launch_monitor_2(ma, kMonitorGrid, ctx->stream); break;
+  }
+  CK(cudaGetLastError());
+  std::vector<double> part((size_t)kMonitorGrid * 3);
+  std::vector<unsigned long long> bad((size_t)kMonitorGrid);
+  CK(cudaMemcpyAsync(part.data(), ctx->d_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(bad.data(), ctx->d_part_bad, sizeof(unsigned long long) * bad.size(),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double mass = 0.0, mx = 0.0, mn = 1.0e300;
+  int64_t nb = 0;
+  for (int k = 0; k < kMonitorGrid; ++k) {
+    mass += part[k];
+    double m = part[kMonitorGrid + k];
+    if (!(m <= mx)) mx = m;
+    mn = std::min(mn, part[2 * kMonitorGrid + k]);
+    nb += (int64_t)bad[k];
+  }
+  out->mass = mass;
+  out->max_du = mx;
+  out->min_f = mn;
+  out->unstable_sites = nb;
+  out->time_step = (int64_t)ctx->t1;
+  return nb ? HLBG_ERR_UNSTABLE : HLBG_OK;
+}
+
+int hlbg_iolet_density(const hlbg_ctx* ctx, int32_t is_outlet, int32_t index, uint64_t t,
+                       double* density) {
+  if (!ctx || !density) return HLBG_ERR_INVAL;
+  const auto& v = is_outlet ? ctx->outlets : ctx->inlets;
+  if (index < 0 || index >= (int32_t)v.size()) return HLBG_ERR_INVAL;
+  *density = iolet_density(ctx, v[index], t);
+  return HLBG_OK;
+}
+
+int hlbg_time_steps(hlbg_ctx* ctx, int32_t nsteps, float* ms) {
+  if (!ctx || !ms) return HLBG_ERR_INVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  int rc = hlbg_step(ctx, nsteps, nullptr);
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  CK(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+  return HLBG_OK;
+}
+
+}  // extern "C"

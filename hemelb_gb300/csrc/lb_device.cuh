@@ -1,0 +1,293 @@
+// Device kernels of the GB300 lattice-Boltzmann update (D3Q19).
+//
+// Layout in HBM (built by layout.cpp):
+//   * non-empty 8^3 blocks in Morton order; slot = block * 512 + local index,
+//     local = (x * 8 + y) * 8 + z, the reference's SiteTraverser order;
+//   * distributions structure-of-arrays, f[d * stride + slot], two copies
+//     (old / new) swapped every step (FieldData::SwapOldAndNew);
+//   * block_nbr[block * 27 + (dx+1)*9 + (dy+1)*3 + (dz+1)] = neighbouring block
+//     index or -1, staged in shared memory per CTA;
+//   * site_code[slot] = 0 solid, 1 bulk (all 18 links fluid-fluid, no wall or
+//     iolet bit), 2 + r for boundary record r;
+//   * boundary records (wall / iolet masks, iolet id, collision type, cut
+//     distances) for the few percent of sites next to a wall or an iolet.
+//
+// One thread collides one site and pushes its 19 post-collision values to the
+// neighbours' slots of f_new (BulkLink, Code/lb/streamers/BulkStreamer.h:142-150),
+// or, for wall and iolet links, into its own slot of the inverse direction
+// (SimpleBounceBack.h:245-254, BouzidiFirdaousLallemand.h:307-334,
+// NashZerothOrderPressure.h:388-421, LaddIolet.h:465-502).  The link precedence is
+// StreamerTypeFactory's (Code/lb/streamers/StreamerTypeFactory.h:65-79): iolet
+// first, then wall, else bulk, with the iolet/wall delegates present only for the
+// collision types that carry them.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace hlbg {
+
+constexpr int Q = 19;
+constexpr int kSites = 512;
+
+static __constant__ int c_cx[Q] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+static __constant__ int c_cy[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+static __constant__ int c_cz[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+static __constant__ int c_inv[Q] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+
+// Compile-time lattice tables for fully unrolled loops (constant-folded).
+struct Lat {
+  __host__ __device__ static constexpr int cx(int i) {
+    constexpr int t[Q] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int cy(int i) {
+    constexpr int t[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int cz(int i) {
+    constexpr int t[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+    return t[i];
+  }
+  __host__ __device__ static constexpr int inv(int i) { return i == 0 ? 0 : (i & 1 ? i + 1 : i - 1); }
+};
+// D3Q19 weights (Code/lb/lattices/D3Q19.h:39-47), as the same double expressions.
+__host__ __device__ constexpr double weight_d(int i) {
+  return i == 0 ? 1.0 / 3.0 : (i < 7 ? 1.0 / 18.0 : 1.0 / 36.0);
+}
+
+// Per-iolet constants on the device.
+struct IoletDev {
+  double pos[3];
+  double n[3];   // normalised normal (InOutLet::SetNormal)
+  double nf[3];  // the normal rounded to float, as double (GetNormal().as<float>())
+  double radius;
+  int32_t model;
+  int32_t pad_;
+};
+
+struct StepArgs {
+  const void* f_old;
+  void* f_new;
+  int64_t stride;  // elements between directions (= slot count)
+  int64_t nslot;
+  const int32_t* block_nbr;
+  const uint32_t* site_code;
+  const uint8_t* block_bulk;  // 1: all 512 slots are bulk sites
+  const uint32_t* b_wall;
+  const uint32_t* b_iolet;
+  const int32_t* b_ioid;
+  const int8_t* b_type;
+  const float* b_cut;  // [nrec * 18] or null
+  const int32_t* list;  // optional slot list (per-range drop-in), null = all slots
+  int64_t list_count;
+  const IoletDev* iolets;     // [n_in + n_out]
+  const double* iolet_rho;    // [n_in + n_out] ghost density for this step (Nash)
+  const double* iolet_umax;   // [n_in + n_out] peak speed for this step (Ladd)
+  int32_t n_in;
+  int32_t kernel;   // 0 LBGK, 1 TRT
+  int32_t wall;     // 0 SBB, 1 BFL
+  int32_t inlet_model, outlet_model;
+  double omega, omega_minus;
+  float omega_f, omega_minus_f;
+  float fp16_scale, fp16_inv_scale;
+};
+
+// ---- storage forms ---------------------------------------------------------
+// FP64: f itself.  FP32DEV / FP16: g = f - w_d (FP16 scaled by fp16_scale).
+template <int P>
+struct Store;
+template <>
+struct Store<0> {
+  using S = double;
+  static __device__ __forceinline__ double load(const S* p, int64_t i, const StepArgs&) {
+    return __ldg(p + i);
+  }
+  static __device__ __forceinline__ void store(S* p, int64_t i, double v, const StepArgs&) {
+    p[i] = v;
+  }
+};
+template <>
+struct Store<1> {
+  using S = float;
+  static __device__ __forceinline__ float load(const S* p, int64_t i, const StepArgs&) {
+    return __ldg(p + i);
+  }
+  static __device__ __forceinline__ void store(S* p, int64_t i, float v, const StepArgs&) {
+    p[i] = v;
+  }
+};
+template <>
+struct Store<2> {
+  using S = __half;
+  static __device__ __forceinline__ float load(const S* p, int64_t i, const StepArgs& a) {
+    return __half2float(__ldg(p + i)) * a.fp16_inv_scale;
+  }
+  static __device__ __forceinline__ void store(S* p, int64_t i, float v, const StepArgs& a) {
+    p[i] = __float2half_rn(v * a.fp16_scale);
+  }
+};
+
+__device__ __forceinline__ int bit(uint32_t m, int d) { return d ? (int)((m >> (d - 1)) & 1u) : 0; }
+
+// Neighbour slot of (block b, local l) along direction d, or -1 if the block is absent.
+__device__ __forceinline__ int64_t nbr_slot(const int32_t* sh_nbr, int l, int d) {
+  int x = (l >> 6) + c_cx[d], y = ((l >> 3) & 7) + c_cy[d], z = (l & 7) + c_cz[d];
+  int ox = (x >> 3), oy = (y >> 3), oz = (z >> 3);  // -1, 0 or 1 (arithmetic shift)
+  int nb = sh_nbr[(ox + 1) * 9 + (oy + 1) * 3 + (oz + 1)];
+  if (nb < 0) return -1;
+  return (int64_t)nb * kSites + (((x & 7) * 8 + (y & 7)) * 8 + (z & 7));
+}
+
+// ---- FP64 collide in the reference's scalar evaluation order ---------------
+// Lattice::CalculateDensityAndMomentum (Code/lb/lattices/Lattice.h:181-191),
+// CalculateFeq (:332-355), LBGK::Collide (Code/lb/kernels/LBGK.h:56-63) and TRT
+// (Code/lb/kernels/TRT.h:160-188).  This translation unit is compiled with
+// --fmad=false so each operation rounds on its own.
+__device__ __forceinline__ void feq64(double rho, double mx, double my, double mz, double* feq) {
+  const double density_1 = 1. / rho;
+  const double m2 = mx * mx + my * my + mz * mz;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const double mde = Lat::cx(i) * mx + Lat::cy(i) * my + Lat::cz(i) * mz;
+    feq[i] = weight_d(i) * (rho - (3. / 2.) * m2 * density_1 + (9. / 2.) * density_1 * mde * mde +
+                            3. * mde);
+  }
+}
+
+__device__ __forceinline__ double feq64_one(double rho, double mx, double my, double mz, int i) {
+  const double density_1 = 1. / rho;
+  const double m2 = mx * mx + my * my + mz * mz;
+  const double mde = c_cx[i] * mx + c_cy[i] * my + c_cz[i] * mz;
+  return weight_d(i) * (rho - (3. / 2.) * m2 * density_1 + (9. / 2.) * density_1 * mde * mde +
+                        3. * mde);
+}
+
+__device__ __forceinline__ void collide64(const StepArgs& a, const double* f, double& rho,
+                                          double& mx, double& my, double& mz, double* fpost) {
+  double r = 0.0, x = 0.0, y = 0.0, z = 0.0;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    r += f[i];
+    x += (double)Lat::cx(i) * f[i];
+    y += (double)Lat::cy(i) * f[i];
+    z += (double)Lat::cz(i) * f[i];
+  }
+  rho = r;
+  mx = x;
+  my = y;
+  mz = z;
+  double feq[Q];
+  feq64(rho, mx, my, mz, feq);
+  if (a.kernel == 0) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) fpost[i] = f[i] + (f[i] - feq[i]) * a.omega;
+  } else {
+    fpost[0] = f[0] + a.omega * (f[0] - feq[0]);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+      const int ib = i + 1;
+      const double ni = f[i] - feq[i], nb = f[ib] - feq[ib];
+      const double sym = 0.5 * a.omega * (ni + nb);
+      const double asym = 0.5 * a.omega_minus * (ni - nb);
+      fpost[i] = f[i] + sym + asym;
+      fpost[ib] = f[ib] + sym - asym;
+    }
+  }
+}
+
+// ---- FP32 collide on deviations g = f - w ----------------------------------
+// Same model (compressible D3Q19 equilibrium, LBGK or TRT); sums are formed on
+// the deviations so that FP32 keeps the small departures from rest.
+__device__ __forceinline__ float weight_f(int i) {
+  return i == 0 ? (float)(1.0 / 3.0) : (i < 7 ? (float)(1.0 / 18.0) : (float)(1.0 / 36.0));
+}
+
+__device__ __forceinline__ void moments_dev(const float* g, float& dr, float& mx, float& my,
+                                            float& mz) {
+  // pairwise grouping by direction families keeps FP32 rounding small
+  dr = g[0] + ((g[1] + g[2]) + (g[3] + g[4]) + (g[5] + g[6])) +
+       (((g[7] + g[8]) + (g[9] + g[10])) + ((g[11] + g[12]) + (g[13] + g[14])) +
+        ((g[15] + g[16]) + (g[17] + g[18])));
+  mx = (g[1] - g[2]) + ((g[7] - g[8]) + (g[9] - g[10])) + ((g[11] - g[12]) + (g[13] - g[14]));
+  my = (g[3] - g[4]) + ((g[7] - g[8]) - (g[9] - g[10])) + ((g[15] - g[16]) + (g[17] - g[18]));
+  mz = (g[5] - g[6]) + ((g[11] - g[12]) - (g[13] - g[14])) + ((g[15] - g[16]) - (g[17] - g[18]));
+}
+
+__device__ __forceinline__ float geq_dev(float dr, float inv_rho, float m2x15, float mx, float my,
+                                         float mz, int i) {
+  const float mde = Lat::cx(i) * mx + Lat::cy(i) * my + Lat::cz(i) * mz;
+  return weight_f(i) * ((dr - m2x15 * inv_rho) + mde * (3.f + 4.5f * inv_rho * mde));
+}
+
+__device__ __forceinline__ void collide_dev(const StepArgs& a, const float* g, float& dr, float& mx,
+                                            float& my, float& mz, float* gpost) {
+  moments_dev(g, dr, mx, my, mz);
+  const float inv_rho = 1.f / (1.f + dr);
+  const float m2x15 = 1.5f * (mx * mx + my * my + mz * mz);
+  if (a.kernel == 0) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      const float ge = geq_dev(dr, inv_rho, m2x15, mx, my, mz, i);
+      gpost[i] = g[i] + a.omega_f * (g[i] - ge);
+    }
+  } else {
+    {
+      const float ge = geq_dev(dr, inv_rho, m2x15, mx, my, mz, 0);
+      gpost[0] = g[0] + a.omega_f * (g[0] - ge);
+    }
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+      const int ib = i + 1;
+      const float ni = g[i] - geq_dev(dr, inv_rho, m2x15, mx, my, mz, i);
+      const float nb = g[ib] - geq_dev(dr, inv_rho, m2x15, mx, my, mz, ib);
+      const float sym = 0.5f * a.omega_f * (ni + nb);
+      const float asym = 0.5f * a.omega_minus_f * (ni - nb);
+      gpost[i] = g[i] + sym + asym;
+      gpost[ib] = g[ib] + sym - asym;
+    }
+  }
+}
+
+// ---- boundary link values ---------------------------------------------------
+// FP64 form: exact reference arithmetic.
+__device__ __forceinline__ double dot3d(double ax, double ay, double az, double bx, double by,
+                                       double bz) {
+  double s = 0.0;  // std::inner_product from RES{0}
+  s = s + ax * bx;
+  s = s + ay * by;
+  s = s + az * bz;
+  return s;
+}
+
+// NashZerothOrderPressureLink::StreamLink (NashZerothOrderPressure.h:388-421)
+__device__ __forceinline__ double nash64(const IoletDev& io, double ghost_rho, double rho, double mx,
+                                         double my, double mz, int unstreamed) {
+  const double component = dot3d(mx, my, mz, io.nf[0], io.nf[1], io.nf[2]) / rho;
+  const double gx = io.nf[0] * component * ghost_rho;
+  const double gy = io.nf[1] * component * ghost_rho;
+  const double gz = io.nf[2] * component * ghost_rho;
+  return feq64_one(ghost_rho, gx, gy, gz, unstreamed);
+}
+
+// InOutLetParabolicVelocity::GetVelocity (InOutLetParabolicVelocity.cc:23-43) at the
+// link midpoint with the step's peak speed, then LaddIoletLink's correction
+// (LaddIolet.h:481-501).
+__device__ __forceinline__ double ladd_correction64(const IoletDev& io, double umax, double rho,
+                                                    int l_x, int l_y, int l_z, int d) {
+  const double hx = (double)l_x + 0.5 * c_cx[d];
+  const double hy = (double)l_y + 0.5 * c_cy[d];
+  const double hz = (double)l_z + 0.5 * c_cz[d];
+  const double dx = hx - io.pos[0], dy = hy - io.pos[1], dz = hz - io.pos[2];
+  const double z = dot3d(dx, dy, dz, io.n[0], io.n[1], io.n[2]);
+  const double rSq = (dot3d(dx, dy, dz, dx, dy, dz) - z * z) / (io.radius * io.radius);
+  const double s = umax * (1. - rSq);
+  double wx = io.n[0] * s, wy = io.n[1] * s, wz = io.n[2] * s;
+  wx *= rho;
+  wy *= rho;
+  wz *= rho;
+  const double dd = dot3d(wx, wy, wz, (double)c_cx[d], (double)c_cy[d], (double)c_cz[d]);
+  return 2. * weight_d(d) * dd / (1.0 / 3.0);
+}
+
+}  // namespace hlbg

@@ -1,0 +1,82 @@
+// Launch interface between the host context (capi.cu) and the kernel
+// translation units (lb_fp64.cu, lb_fp32.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hlbg {
+
+struct StepArgs;
+
+struct PostArgs {
+  void* f_new;
+  int64_t stride;
+  const int32_t* slot;
+  const int8_t* dir;
+  const float* q;
+  int64_t count;
+  float fp16_scale, fp16_inv_scale;
+};
+
+struct InitArgs {
+  void* f0;
+  void* f1;
+  int64_t stride, nslot;
+  const uint32_t* site_code;
+  const uint8_t* block_bulk;
+  double value[19];
+  float fp16_scale, fp16_inv_scale;
+};
+
+struct FieldArgs {
+  void* f0;
+  void* f1;
+  int64_t stride;
+  const int32_t* ref2slot;
+  int64_t first, count;
+  const double* rho;  // [count]
+  const double* u;    // [count*3]
+  float fp16_scale, fp16_inv_scale;
+};
+
+struct GatherArgs {
+  const void* f;
+  void* f_out;
+  int64_t stride;
+  const int32_t* ref2slot;
+  int64_t first, count;
+  double* aos;  // [count*19]
+  double* rho;  // [count]
+  double* u;    // [count*3]
+  float fp16_scale, fp16_inv_scale;
+};
+
+struct MonitorArgs {
+  const void* f_cur;
+  const void* f_prev;
+  int64_t stride, nslot;
+  const uint32_t* site_code;
+  const uint8_t* block_bulk;
+  double* part_mass;
+  double* part_max;
+  double* part_min;
+  unsigned long long* part_bad;
+  float fp16_scale, fp16_inv_scale;
+};
+
+#define HLBG_DECLARE(P)                                                              \
+  void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st); \
+  void launch_post_step_##P(const PostArgs& p, cudaStream_t st);                     \
+  void launch_init_uniform_##P(const InitArgs& ia, cudaStream_t st);                 \
+  void launch_init_field_##P(const FieldArgs& fa, cudaStream_t st);                  \
+  void launch_gather_##P(const GatherArgs& ga, cudaStream_t st);                     \
+  void launch_scatter_##P(const GatherArgs& ga, cudaStream_t st);                    \
+  void launch_macro_##P(const GatherArgs& ga, cudaStream_t st);                      \
+  void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st);
+
+HLBG_DECLARE(0)
+HLBG_DECLARE(1)
+HLBG_DECLARE(2)
+
+}  // namespace hlbg

@@ -1,0 +1,622 @@
+// Seeded synthetic vessel geometries in HemeLB's sparse-block form.
+//
+// The output is what a GmyReadResult holds after GeometryReader::LoadAndDecompose
+// (Code/geometry/GeometryReader.cc:80-166, ParseSite :556-657) for the links the
+// LB update reads: per non-empty 8^3 block a fluid bitmap, and for every fluid
+// site with a solid neighbour its wall/iolet link masks, iolet id, site type and
+// cut distances.  SiteData semantics follow Code/geometry/SiteDataBare.cc:18-68:
+// the iolet id is that of the last iolet link in direction order, and the site
+// type is INLET if any link is an inlet link, else OUTLET if any is an outlet
+// link, else FLUID.
+//
+// Shapes are unions of cylinders with optional spherical end caps (vessel
+// segments and junctions) and z-aligned stenosed pipes with a Gaussian
+// narrowing.  A voxel centre (integer coordinates) is fluid when it lies inside
+// the union, inside the box, and not beyond any iolet plane.  A link from a
+// fluid site to a non-fluid site is an iolet link when its end point lies beyond
+// an iolet plane (iolets are tested before walls, as StreamerTypeFactory does),
+// otherwise a wall link.  Cut distances are fractions of the link length, the
+// convention of geometry-tool's CylinderGenerator
+// (geometry-tool/HlbGmyTool/Model/Generation/CylinderGenerator.cpp:265-268):
+// exact for iolet planes, and for walls the root of the analytic inside-test
+// along the link found by bisection to 1e-12 and stored as float (as .gmy does).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <thread>
+#include <vector>
+
+#include "../../include/hemelb_gb300.h"
+
+namespace {
+
+constexpr int kBlock = 8;
+constexpr int kSitesPerBlock = 512;
+
+const int CX19[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+const int CY19[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+const int CZ19[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+// D3Q15 (Code/lb/lattices/D3Q15.h): rest, 6 faces, 8 corners.
+const int CX15[15] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+const int CY15[15] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, -1, 1, -1, 1};
+const int CZ15[15] = {0, 0, 0, 0, 0, 1, -1, 1, -1, -1, 1, 1, -1, -1, 1};
+
+struct Vec {
+  double x, y, z;
+};
+inline Vec add(Vec a, Vec b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline Vec sub(Vec a, Vec b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline Vec mul(Vec a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline double dot(Vec a, Vec b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline Vec cross(Vec a, Vec b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline Vec normalised(Vec a) { return mul(a, 1.0 / std::sqrt(dot(a, a))); }
+
+struct Shape {
+  int kind;  // 0 = cylinder segment (optional caps), 1 = stenosed z pipe
+  Vec a, b;
+  double r;
+  bool cap_a, cap_b;
+  double depth, zc, sigma;  // stenosis
+  Vec lo, hi;               // bounding box
+};
+
+struct Iolet {
+  int outlet;  // 0 inlet, 1 outlet
+  int index;   // index in its own list
+  Vec pos, n;  // n points into the fluid
+  double radius;
+  Vec lo, hi;
+};
+
+bool inside_shape(const Shape& s, Vec p) {
+  if (s.kind == 0) {
+    Vec v = sub(s.b, s.a);
+    Vec w = sub(p, s.a);
+    double l2 = dot(v, v);
+    double t = dot(w, v) / l2;
+    double r2 = s.r * s.r;
+    if (t < 0.0) return s.cap_a && dot(w, w) < r2;
+    if (t > 1.0) {
+      Vec u = sub(p, s.b);
+      return s.cap_b && dot(u, u) < r2;
+    }
+    Vec perp = sub(w, mul(v, t));
+    return dot(perp, perp) < r2;
+  }
+  // stenosed pipe along z from a.z to b.z, axis through (a.x, a.y)
+  if (p.z < s.a.z || p.z > s.b.z) return false;
+  double dz = p.z - s.zc;
+  double rr = s.r * (1.0 - s.depth * std::exp(-dz * dz / (2.0 * s.sigma * s.sigma)));
+  double dx = p.x - s.a.x, dy = p.y - s.a.y;
+  return dx * dx + dy * dy < rr * rr;
+}
+
+// Signed distance of p from the iolet plane (positive on the fluid side).
+inline double iolet_side(const Iolet& io, Vec p) { return dot(sub(p, io.pos), io.n); }
+
+bool beyond_iolet(const Iolet& io, Vec p) {
+  double s = iolet_side(io, p);
+  if (s >= 0.0 || s < -4.0) return false;
+  Vec lat = sub(sub(p, io.pos), mul(io.n, s));
+  double lim = io.radius * 1.15 + 1.5;
+  return dot(lat, lat) < lim * lim;
+}
+
+struct Geometry {
+  int q = 19;
+  int nb[3] = {0, 0, 0};
+  std::vector<Shape> shapes;
+  std::vector<Iolet> inlets, outlets;
+  // outputs
+  std::vector<int32_t> block_coords;
+  std::vector<uint64_t> fluid_mask;
+  std::vector<int64_t> link_site;
+  std::vector<uint32_t> wall_mask, iolet_mask;
+  std::vector<int32_t> iolet_id;
+  std::vector<int8_t> site_type;
+  std::vector<float> cuts;
+  int64_t n_fluid = 0;
+  bool with_cuts = false;
+};
+
+uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+  // x is the most significant bit of each triple (Code/geometry/LookupTree.h:23-41)
+  uint64_t m = 0;
+  for (int k = 0; k < 16; ++k) {
+    m |= (uint64_t)((x >> k) & 1u) << (3 * k + 2);
+    m |= (uint64_t)((y >> k) & 1u) << (3 * k + 1);
+    m |= (uint64_t)((z >> k) & 1u) << (3 * k);
+  }
+  return m;
+}
+
+struct BlockOut {
+  uint64_t mask[8];
+  std::vector<int32_t> local;
+  std::vector<uint32_t> wall, iolet;
+  std::vector<int32_t> ioid;
+  std::vector<int8_t> stype;
+  std::vector<float> cuts;
+  int64_t nfluid = 0;
+};
+
+struct Voxelizer {
+  Geometry& g;
+  const int* cx;
+  const int* cy;
+  const int* cz;
+  // macro grid of 8x8x8 blocks for candidate culling
+  int mg[3];
+  std::vector<std::vector<int>> cell_shapes, cell_iolets;  // iolet ids: inlets 0.., outlets offset
+  Voxelizer(Geometry& geo) : g(geo) {
+    if (g.q == 15) {
+      cx = CX15; cy = CY15; cz = CZ15;
+    } else {
+      cx = CX19; cy = CY19; cz = CZ19;
+    }
+    for (int a = 0; a < 3; ++a) mg[a] = (g.nb[a] + 7) / 8;
+    cell_shapes.resize((size_t)mg[0] * mg[1] * mg[2]);
+    cell_iolets.resize(cell_shapes.size());
+    auto bin = [&](Vec lo, Vec hi, std::vector<std::vector<int>>& lists, int id) {
+      int c0[3], c1[3];
+      double l[3] = {lo.x - 2, lo.y - 2, lo.z - 2}, h[3] = {hi.x + 2, hi.y + 2, hi.z + 2};
+      for (int a = 0; a < 3; ++a) {
+        c0[a] = std::max(0, (int)std::floor(l[a] / 64.0));
+        c1[a] = std::min(mg[a] - 1, (int)std::floor(h[a] / 64.0));
+      }
+      for (int i = c0[0]; i <= c1[0]; ++i)
+        for (int j = c0[1]; j <= c1[1]; ++j)
+          for (int k = c0[2]; k <= c1[2]; ++k)
+            lists[((size_t)i * mg[1] + j) * mg[2] + k].push_back(id);
+    };
+    for (int s = 0; s < (int)g.shapes.size(); ++s) bin(g.shapes[s].lo, g.shapes[s].hi, cell_shapes, s);
+    for (int s = 0; s < (int)g.inlets.size(); ++s) bin(g.inlets[s].lo, g.inlets[s].hi, cell_iolets, s);
+    for (int s = 0; s < (int)g.outlets.size(); ++s)
+      bin(g.outlets[s].lo, g.outlets[s].hi, cell_iolets, (int)g.inlets.size() + s);
+  }
+  const Iolet& iolet_by(int id) const {
+    return id < (int)g.inlets.size() ? g.inlets[id] : g.outlets[id - g.inlets.size()];
+  }
+  bool in_box(Vec p) const {
+    return p.x >= -0.5 && p.y >= -0.5 && p.z >= -0.5 && p.x <= g.nb[0] * kBlock - 0.5 &&
+           p.y <= g.nb[1] * kBlock - 0.5 && p.z <= g.nb[2] * kBlock - 0.5;
+  }
+  bool in_union(const std::vector<int>& shp, Vec p) const {
+    for (int s : shp)
+      if (inside_shape(g.shapes[s], p)) return true;
+    return false;
+  }
+  bool fluid(const std::vector<int>& shp, const std::vector<int>& iol, Vec p) const {
+    if (!in_box(p)) return false;
+    if (!in_union(shp, p)) return false;
+    for (int i : iol)
+      if (beyond_iolet(iolet_by(i), p)) return false;
+    return true;
+  }
+
+  void block(int bx, int by, int bz, BlockOut& out) const {
+    std::memset(out.mask, 0, sizeof(out.mask));
+    size_t cell = ((size_t)(bx / 8) * mg[1] + by / 8) * mg[2] + bz / 8;
+    const auto& shp = cell_shapes[cell];
+    const auto& iol = cell_iolets[cell];
+    if (shp.empty()) return;
+    // quick reject: block AABB vs candidate shapes' boxes
+    double o[3] = {(double)bx * kBlock, (double)by * kBlock, (double)bz * kBlock};
+    bool any = false;
+    for (int s : shp) {
+      const Shape& S = g.shapes[s];
+      if (S.hi.x < o[0] - 1.5 || S.lo.x > o[0] + 8.5 || S.hi.y < o[1] - 1.5 ||
+          S.lo.y > o[1] + 8.5 || S.hi.z < o[2] - 1.5 || S.lo.z > o[2] + 8.5)
+        continue;
+      any = true;
+      break;
+    }
+    if (!any) return;
+    // fluid flags on a 10^3 halo grid
+    uint8_t fl[10][10][10];
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j)
+        for (int k = 0; k < 10; ++k)
+          fl[i][j][k] = fluid(shp, iol, Vec{o[0] + i - 1, o[1] + j - 1, o[2] + k - 1});
+    const int nl = g.q - 1;
+    for (int i = 0; i < 8; ++i)
+      for (int j = 0; j < 8; ++j)
+        for (int k = 0; k < 8; ++k) {
+          if (!fl[i + 1][j + 1][k + 1]) continue;
+          int l = (i * 8 + j) * 8 + k;
+          out.mask[l >> 6] |= 1ull << (l & 63);
+          out.nfluid++;
+          uint32_t wm = 0, im = 0;
+          int ioid = -1;
+          bool had_in = false, had_out = false;
+          float cutv[26];
+          for (int d = 1; d <= nl; ++d) cutv[d - 1] = -1.0f;  // NO_VALUE-like for fluid links
+          Vec p{o[0] + i, o[1] + j, o[2] + k};
+          for (int d = 1; d <= nl; ++d) {
+            if (fl[i + 1 + cx[d]][j + 1 + cy[d]][k + 1 + cz[d]]) continue;
+            Vec c{(double)cx[d], (double)cy[d], (double)cz[d]};
+            Vec pe = add(p, c);
+            int hit = -1;
+            for (int ii : iol)
+              if (beyond_iolet(iolet_by(ii), pe)) {
+                hit = ii;
+                break;
+              }
+            if (hit >= 0) {
+              const Iolet& io = iolet_by(hit);
+              im |= 1u << (d - 1);
+              ioid = io.index;
+              if (io.outlet) had_out = true; else had_in = true;
+              double s0 = iolet_side(io, p), s1 = iolet_side(io, pe);
+              cutv[d - 1] = (float)(s0 / (s0 - s1));
+            } else {
+              wm |= 1u << (d - 1);
+              if (g.with_cuts) {
+                double t0 = 0.0, t1 = 1.0;
+                for (int it = 0; it < 48 && t1 - t0 > 1e-12; ++it) {
+                  double tm = 0.5 * (t0 + t1);
+                  Vec pm = add(p, mul(c, tm));
+                  if (in_box(pm) && in_union(shp, pm)) t0 = tm; else t1 = tm;
+                }
+                double qv = 0.5 * (t0 + t1);
+                if (qv < 1e-6) qv = 1e-6;
+                cutv[d - 1] = (float)qv;
+              }
+            }
+          }
+          if (wm == 0 && im == 0) continue;
+          out.local.push_back(l);
+          out.wall.push_back(wm);
+          out.iolet.push_back(im);
+          out.ioid.push_back(ioid);
+          out.stype.push_back(had_in ? HLBG_SITE_INLET : (had_out ? HLBG_SITE_OUTLET : HLBG_SITE_FLUID));
+          if (g.with_cuts)
+            for (int d = 0; d < nl; ++d) out.cuts.push_back(cutv[d]);
+        }
+  }
+};
+
+void shape_bounds(Shape& s) {
+  if (s.kind == 0) {
+    double r = s.r + 1.0;
+    s.lo = {std::min(s.a.x, s.b.x) - r, std::min(s.a.y, s.b.y) - r, std::min(s.a.z, s.b.z) - r};
+    s.hi = {std::max(s.a.x, s.b.x) + r, std::max(s.a.y, s.b.y) + r, std::max(s.a.z, s.b.z) + r};
+  } else {
+    double r = s.r + 1.0;
+    s.lo = {s.a.x - r, s.a.y - r, s.a.z - 1.0};
+    s.hi = {s.a.x + r, s.a.y + r, s.b.z + 1.0};
+  }
+}
+void iolet_bounds(Iolet& io) {
+  double r = io.radius * 1.15 + 6.0;
+  io.lo = {io.pos.x - r, io.pos.y - r, io.pos.z - r};
+  io.hi = {io.pos.x + r, io.pos.y + r, io.pos.z + r};
+}
+
+// Translate everything by an integer offset so the bounding box starts at 2 and
+// choose the block counts.
+void place(Geometry& g, int fixed_box_sites) {
+  if (fixed_box_sites > 0) {
+    for (int a = 0; a < 3; ++a) g.nb[a] = fixed_box_sites / kBlock;
+  } else {
+    Vec lo{1e30, 1e30, 1e30}, hi{-1e30, -1e30, -1e30};
+    for (auto& s : g.shapes) {
+      shape_bounds(s);
+      lo = {std::min(lo.x, s.lo.x), std::min(lo.y, s.lo.y), std::min(lo.z, s.lo.z)};
+      hi = {std::max(hi.x, s.hi.x), std::max(hi.y, s.hi.y), std::max(hi.z, s.hi.z)};
+    }
+    Vec off{2.0 - std::floor(lo.x), 2.0 - std::floor(lo.y), 2.0 - std::floor(lo.z)};
+    for (auto& s : g.shapes) {
+      s.a = add(s.a, off);
+      s.b = add(s.b, off);
+      if (s.kind == 1) s.zc += off.z;
+    }
+    for (auto* v : {&g.inlets, &g.outlets})
+      for (auto& io : *v) io.pos = add(io.pos, off);
+    double ext[3] = {hi.x + off.x + 3.0, hi.y + off.y + 3.0, hi.z + off.z + 3.0};
+    for (int a = 0; a < 3; ++a) g.nb[a] = (int)std::ceil(ext[a] / kBlock);
+  }
+  for (auto& s : g.shapes) shape_bounds(s);
+  for (auto* v : {&g.inlets, &g.outlets})
+    for (auto& io : *v) iolet_bounds(io);
+}
+
+int voxelize(Geometry& g, int n_threads) {
+  Voxelizer vx(g);
+  // candidate blocks: those touched by a shape's box
+  std::vector<uint8_t> cand((size_t)g.nb[0] * g.nb[1] * g.nb[2], 0);
+  for (auto& s : g.shapes) {
+    int b0[3], b1[3];
+    double l[3] = {s.lo.x - 1, s.lo.y - 1, s.lo.z - 1}, h[3] = {s.hi.x + 1, s.hi.y + 1, s.hi.z + 1};
+    for (int a = 0; a < 3; ++a) {
+      b0[a] = std::max(0, (int)std::floor(l[a] / kBlock));
+      b1[a] = std::min(g.nb[a] - 1, (int)std::floor(h[a] / kBlock));
+    }
+    for (int i = b0[0]; i <= b1[0]; ++i)
+      for (int j = b0[1]; j <= b1[1]; ++j)
+        for (int k = b0[2]; k <= b1[2]; ++k) cand[((size_t)i * g.nb[1] + j) * g.nb[2] + k] = 1;
+  }
+  std::vector<std::pair<uint64_t, uint32_t>> order;  // (morton, block id)
+  for (int i = 0; i < g.nb[0]; ++i)
+    for (int j = 0; j < g.nb[1]; ++j)
+      for (int k = 0; k < g.nb[2]; ++k) {
+        size_t id = ((size_t)i * g.nb[1] + j) * g.nb[2] + k;
+        if (cand[id]) order.push_back({morton3(i, j, k), (uint32_t)id});
+      }
+  std::sort(order.begin(), order.end());
+  std::vector<BlockOut> outs(order.size());
+  std::atomic<size_t> next{0};
+  if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  auto work = [&]() {
+    for (;;) {
+      size_t c = next.fetch_add(64);
+      if (c >= order.size()) break;
+      size_t e = std::min(order.size(), c + 64);
+      for (size_t t = c; t < e; ++t) {
+        uint32_t id = order[t].second;
+        int k = id % g.nb[2];
+        int j = (id / g.nb[2]) % g.nb[1];
+        int i = id / ((size_t)g.nb[2] * g.nb[1]);
+        vx.block(i, j, k, outs[t]);
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < n_threads; ++t) th.emplace_back(work);
+  work();
+  for (auto& t : th) t.join();
+  for (size_t t = 0; t < order.size(); ++t) {
+    BlockOut& b = outs[t];
+    if (b.nfluid == 0) continue;
+    uint32_t id = order[t].second;
+    int64_t bi = (int64_t)g.block_coords.size() / 3;
+    g.block_coords.push_back(id / (g.nb[2] * g.nb[1]));
+    g.block_coords.push_back((id / g.nb[2]) % g.nb[1]);
+    g.block_coords.push_back(id % g.nb[2]);
+    for (int w = 0; w < 8; ++w) g.fluid_mask.push_back(b.mask[w]);
+    g.n_fluid += b.nfluid;
+    for (size_t s = 0; s < b.local.size(); ++s) {
+      g.link_site.push_back(bi * kSitesPerBlock + b.local[s]);
+      g.wall_mask.push_back(b.wall[s]);
+      g.iolet_mask.push_back(b.iolet[s]);
+      g.iolet_id.push_back(b.ioid[s]);
+      g.site_type.push_back(b.stype[s]);
+    }
+    if (g.with_cuts) g.cuts.insert(g.cuts.end(), b.cuts.begin(), b.cuts.end());
+    outs[t] = BlockOut();
+  }
+  return HLBG_OK;
+}
+
+Shape cyl(Vec a, Vec b, double r, bool ca, bool cb) {
+  Shape s{};
+  s.kind = 0;
+  s.a = a;
+  s.b = b;
+  s.r = r;
+  s.cap_a = ca;
+  s.cap_b = cb;
+  return s;
+}
+Iolet mk_iolet(int outlet, int index, Vec pos, Vec n, double r) {
+  Iolet io{};
+  io.outlet = outlet;
+  io.index = index;
+  io.pos = pos;
+  io.n = normalised(n);
+  io.radius = r;
+  return io;
+}
+
+// Unit vector at angle theta from dir, azimuth phi around it.
+Vec deflect(Vec dir, double theta, double phi) {
+  Vec helper = std::fabs(dir.x) < 0.9 ? Vec{1, 0, 0} : Vec{0, 1, 0};
+  Vec e1 = normalised(cross(dir, helper));
+  Vec e2 = cross(dir, e1);
+  Vec lat = add(mul(e1, std::cos(phi)), mul(e2, std::sin(phi)));
+  return normalised(add(mul(dir, std::cos(theta)), mul(lat, std::sin(theta))));
+}
+
+int finish(Geometry* g, int n_threads, void** handle) {
+  int rc = voxelize(*g, n_threads);
+  if (rc != HLBG_OK) {
+    delete g;
+    return rc;
+  }
+  *handle = g;
+  return HLBG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hlbg_synth_pipe(double radius, int32_t length, int32_t q, int32_t with_cuts, void** handle) {
+  if (!handle || radius <= 0 || length < 1 || (q != 15 && q != 19)) return HLBG_ERR_INVAL;
+  auto* g = new Geometry();
+  g->q = q;
+  g->with_cuts = with_cuts != 0;
+  g->shapes.push_back(cyl({0, 0, -0.5}, {0, 0, length + 0.5}, radius, false, false));
+  g->inlets.push_back(mk_iolet(0, 0, {0, 0, -0.5}, {0, 0, 1}, radius));
+  g->outlets.push_back(mk_iolet(1, 0, {0, 0, length + 0.5}, {0, 0, -1}, radius));
+  place(*g, 0);
+  return finish(g, 0, handle);
+}
+
+int hlbg_synth_stenosis(double radius, int32_t length, double depth, int32_t q, int32_t with_cuts,
+                        void** handle) {
+  if (!handle || radius <= 0 || length < 4 || depth < 0 || depth >= 1 || (q != 15 && q != 19))
+    return HLBG_ERR_INVAL;
+  auto* g = new Geometry();
+  g->q = q;
+  g->with_cuts = with_cuts != 0;
+  Shape s{};
+  s.kind = 1;
+  s.a = {0, 0, -0.5};
+  s.b = {0, 0, length + 0.5};
+  s.r = radius;
+  s.depth = depth;
+  s.zc = 0.5 * length;
+  s.sigma = std::max(2.0, radius);
+  g->shapes.push_back(s);
+  g->inlets.push_back(mk_iolet(0, 0, {0, 0, -0.5}, {0, 0, 1}, radius));
+  g->outlets.push_back(mk_iolet(1, 0, {0, 0, length + 0.5}, {0, 0, -1}, radius));
+  place(*g, 0);
+  return finish(g, 0, handle);
+}
+
+int hlbg_synth_bifurcation(uint64_t seed, double parent_radius, double parent_length,
+                           double daughter_length_factor, int32_t q, int32_t with_cuts,
+                           void** handle) {
+  if (!handle || parent_radius <= 0 || parent_length <= 0 || (q != 15 && q != 19))
+    return HLBG_ERR_INVAL;
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  double split = 0.3 + 0.4 * U(rng);
+  double half = (25.0 + 35.0 * U(rng)) * M_PI / 180.0;
+  double r1 = parent_radius * std::cbrt(split), r2 = parent_radius * std::cbrt(1.0 - split);
+  auto* g = new Geometry();
+  g->q = q;
+  g->with_cuts = with_cuts != 0;
+  Vec a{0, 0, -0.5}, b{0, 0, parent_length};
+  g->shapes.push_back(cyl(a, b, parent_radius, false, true));
+  g->inlets.push_back(mk_iolet(0, 0, a, {0, 0, 1}, parent_radius));
+  double ld = daughter_length_factor * parent_length;
+  Vec d1{std::sin(half), 0, std::cos(half)}, d2{-std::sin(half), 0, std::cos(half)};
+  Vec e1 = add(b, mul(d1, ld)), e2 = add(b, mul(d2, ld));
+  g->shapes.push_back(cyl(b, e1, r1, true, false));
+  g->shapes.push_back(cyl(b, e2, r2, true, false));
+  g->outlets.push_back(mk_iolet(1, 0, e1, mul(d1, -1.0), r1));
+  g->outlets.push_back(mk_iolet(1, 1, e2, mul(d2, -1.0), r2));
+  place(*g, 0);
+  return finish(g, 0, handle);
+}
+
+int hlbg_synth_tree(uint64_t seed, int32_t box_sites, int32_t n_roots, int32_t depth,
+                    double root_radius, int32_t q, int32_t with_cuts, int32_t n_threads,
+                    void** handle) {
+  if (!handle || box_sites < 64 || box_sites % kBlock || n_roots < 1 || depth < 0 || depth > 12 ||
+      root_radius <= 1 || (q != 15 && q != 19))
+    return HLBG_ERR_INVAL;
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  auto* g = new Geometry();
+  g->q = q;
+  g->with_cuts = with_cuts != 0;
+  const double B = box_sites;
+  const double margin = 4.0;
+  auto clip_len = [&](Vec p, Vec d, double len) {
+    // largest t <= len keeping p + t d inside [margin, B-1-margin]^3
+    double t = len;
+    double pc[3] = {p.x, p.y, p.z}, dc[3] = {d.x, d.y, d.z};
+    for (int a = 0; a < 3; ++a) {
+      if (dc[a] > 1e-12) t = std::min(t, (B - 1 - margin - pc[a]) / dc[a]);
+      if (dc[a] < -1e-12) t = std::min(t, (margin - pc[a]) / dc[a]);
+    }
+    return std::max(0.0, t);
+  };
+  struct Seg {
+    Vec start, dir;
+    double r;
+    int level;
+  };
+  int n_out = 0;
+  for (int root = 0; root < n_roots; ++root) {
+    // roots enter through the z=0 face on a jittered grid, pointing inwards
+    int gside = (int)std::ceil(std::sqrt((double)n_roots));
+    int gi = root % gside, gj = root / gside;
+    double cxr = B * (gi + 0.5) / gside + (U(rng) - 0.5) * B * 0.1 / gside;
+    double cyr = B * (gj + 0.5) / gside + (U(rng) - 0.5) * B * 0.1 / gside;
+    double rr = root_radius;
+    cxr = std::min(std::max(cxr, rr + margin + 2), B - rr - margin - 3);
+    cyr = std::min(std::max(cyr, rr + margin + 2), B - rr - margin - 3);
+    Vec start{cxr, cyr, margin};
+    Vec dir = deflect({0, 0, 1}, 10.0 * M_PI / 180.0 * U(rng), 2 * M_PI * U(rng));
+    g->inlets.push_back(mk_iolet(0, root, start, dir, rr));
+    std::vector<Seg> stack{{start, dir, rr, 0}};
+    while (!stack.empty()) {
+      Seg s = stack.back();
+      stack.pop_back();
+      double len = (6.0 + 4.0 * U(rng)) * s.r;
+      double l = clip_len(s.start, s.dir, len);
+      bool leaf = s.level >= depth || l < 2.0 * s.r;
+      if (l < 1.0) l = 1.0;
+      Vec end = add(s.start, mul(s.dir, l));
+      g->shapes.push_back(cyl(s.start, end, s.r, s.level > 0, !leaf));
+      if (leaf) {
+        g->outlets.push_back(mk_iolet(1, n_out++, end, mul(s.dir, -1.0), s.r));
+        continue;
+      }
+      double split = 0.3 + 0.4 * U(rng);
+      double r1 = s.r * std::cbrt(split), r2 = s.r * std::cbrt(1.0 - split);
+      double phi = 2 * M_PI * U(rng);
+      double th1 = (20.0 + 50.0 * U(rng)) * M_PI / 180.0;
+      double th2 = (20.0 + 50.0 * U(rng)) * M_PI / 180.0;
+      Vec d1 = deflect(s.dir, th1, phi), d2 = deflect(s.dir, th2, phi + M_PI);
+      // steer children that would leave the box straight away back towards the centre
+      Vec centre{B / 2, B / 2, B / 2};
+      for (Vec* d : {&d1, &d2}) {
+        if (clip_len(end, *d, 6.0 * s.r) < 3.0 * s.r) {
+          Vec to_c = normalised(sub(centre, end));
+          *d = normalised(add(*d, mul(to_c, 1.5)));
+        }
+      }
+      stack.push_back({end, d2, r2, s.level + 1});
+      stack.push_back({end, d1, r1, s.level + 1});
+    }
+  }
+  place(*g, box_sites);
+  return finish(g, n_threads, handle);
+}
+
+int hlbg_synth_view(void* handle, hlbg_geometry* out, int64_t* n_fluid, int32_t* n_in,
+                    int32_t* n_outl) {
+  if (!handle || !out) return HLBG_ERR_INVAL;
+  auto* g = static_cast<Geometry*>(handle);
+  std::memset(out, 0, sizeof(*out));
+  out->q = g->q;
+  out->block_size = kBlock;
+  for (int a = 0; a < 3; ++a) out->blocks[a] = g->nb[a];
+  out->n_blocks = (int64_t)g->block_coords.size() / 3;
+  out->block_coords = g->block_coords.data();
+  out->fluid_mask = g->fluid_mask.data();
+  out->n_link_sites = (int64_t)g->link_site.size();
+  out->link_site = g->link_site.data();
+  out->wall_mask = g->wall_mask.data();
+  out->iolet_mask = g->iolet_mask.data();
+  out->iolet_id = g->iolet_id.data();
+  out->site_type = g->site_type.data();
+  out->cut_distance = g->with_cuts ? g->cuts.data() : nullptr;
+  out->wall_normal = nullptr;
+  if (n_fluid) *n_fluid = g->n_fluid;
+  if (n_in) *n_in = (int32_t)g->inlets.size();
+  if (n_outl) *n_outl = (int32_t)g->outlets.size();
+  return HLBG_OK;
+}
+
+int hlbg_synth_iolet(void* handle, int32_t is_outlet, int32_t index, double position[3],
+                     double normal[3], double* radius) {
+  if (!handle) return HLBG_ERR_INVAL;
+  auto* g = static_cast<Geometry*>(handle);
+  const auto& v = is_outlet ? g->outlets : g->inlets;
+  if (index < 0 || index >= (int)v.size()) return HLBG_ERR_INVAL;
+  const Iolet& io = v[index];
+  position[0] = io.pos.x;
+  position[1] = io.pos.y;
+  position[2] = io.pos.z;
+  normal[0] = io.n.x;
+  normal[1] = io.n.y;
+  normal[2] = io.n.z;
+  if (radius) *radius = io.radius;
+  return HLBG_OK;
+}
+
+void hlbg_synth_free(void* handle) { delete static_cast<Geometry*>(handle); }
+
+}  // extern "C"

@@ -1,0 +1,227 @@
+/*
+ * hemelb_gb300.h -- C ABI of the GB300-native lattice-Boltzmann update.
+ *
+ * This library replaces HemeLB's per-step LB sweep (lb::LBM<Traits>::PreSend /
+ * PreReceive / PostReceive over the six collision-type site ranges, with the
+ * D3Q19 LBGK/TRT kernels, BulkStreamer, SimpleBounceBack, Bouzidi-Firdaouss-
+ * Lallemand, Nash zeroth-order pressure and Ladd velocity link streamers).
+ * Every entry point takes plain pointers and sizes; the context owns all device
+ * memory; host pointers are borrowed for the duration of the call only.
+ *
+ * Reference interfaces each entry point stands in for (paths within HemeLB):
+ *   hlbg_create            geometry::Domain(latInfo, GmyReadResult, comms) +
+ *                          geometry::FieldData(domain) + LBM::Initialise
+ *                          (Code/geometry/Domain.cc:26-51, Code/geometry/FieldData.cc:14-25,
+ *                           Code/lb/lb.hpp:116-124, InitCollisions :75-114)
+ *   hlbg_init_equilibrium  EquilibriumInitialCondition::SetFs (Code/lb/InitialCondition.hpp:40-52)
+ *   hlbg_step              one SimulationMaster::DoTimeStep LB part: PreSend + PreReceive +
+ *                          PostReceive + FieldData::SwapOldAndNew + SimulationState::Increment
+ *                          (Code/lb/lb.hpp:176-309, Code/SimulationMaster.impl.h:218-219)
+ *   hlbg_stream_and_collide_range / hlbg_post_step_range
+ *                          streamer::StreamAndCollide / PostStep(firstIndex, siteCount, ...)
+ *                          (Code/lb/streamers/StreamerTypeFactory.h:48-108, BulkStreamer.h:178-208)
+ *   hlbg_swap              FieldData::SwapOldAndNew (Code/geometry/FieldData.h:165-167)
+ *   hlbg_get_f / hlbg_put_f FieldData::GetFOld/GetFNew over the contiguous site ids
+ *                          (Code/geometry/FieldData.h:117-160)
+ *   hlbg_get_macro         MacroscopicPropertyCache density/velocity fill
+ *                          (Code/lb/streamers/Common.h:20-42)
+ *   hlbg_reduce            StabilityTester::PostSendToParent + ComputeRelativeDifference
+ *                          (Code/lb/StabilityTester.h:91-183) plus mass / iolet flux
+ *   hlbg_last_error        hemelb::Exception what() (Code/Exception.h)
+ */
+#ifndef HEMELB_GB300_H
+#define HEMELB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (0 = ok) ------------------------------------------------ */
+#define HLBG_OK 0
+#define HLBG_ERR_INVAL 1    /* bad argument or inconsistent geometry            */
+#define HLBG_ERR_OOM 2      /* device or host allocation failed                 */
+#define HLBG_ERR_CUDA 3     /* a CUDA call failed (message in hlbg_last_error)  */
+#define HLBG_ERR_UNSTABLE 4 /* a distribution became <= 0 or NaN (StabilityTester) */
+#define HLBG_ERR_TIMEOUT 5  /* a bounded device wait gave up                    */
+#define HLBG_ERR_STATE 6    /* call not valid in the context's current state    */
+
+/* ---- physics selection (the Traits<> of Code/Traits.h:17-39) --------------- */
+#define HLBG_KERNEL_LBGK 0 /* Code/lb/kernels/LBGK.h */
+#define HLBG_KERNEL_TRT 1  /* Code/lb/kernels/TRT.h, magic Lambda = 3/16 */
+
+#define HLBG_WALL_SBB 0 /* Code/lb/streamers/SimpleBounceBack.h */
+#define HLBG_WALL_BFL 1 /* Code/lb/streamers/BouzidiFirdaousLallemand.h */
+
+#define HLBG_IOLET_NASH 0 /* Code/lb/streamers/NashZerothOrderPressure.h */
+#define HLBG_IOLET_LADD 1 /* Code/lb/streamers/LaddIolet.h */
+
+/* storage form of the distributions on the device */
+#define HLBG_FP64 0    /* plain form: whole update in FP64                         */
+#define HLBG_FP32DEV 1 /* f - w_d stored in FP32, collide in FP32                  */
+#define HLBG_FP16 2    /* f - w_d stored in FP16, collide in FP32                  */
+
+/* iolet value models (Code/lb/iolets) */
+#define HLBG_IOLET_COSINE 0    /* InOutLetCosine: density(t) = mean + amp cos(2 pi t/T + phase) */
+#define HLBG_IOLET_PARABOLIC 1 /* InOutLetParabolicVelocity: n umax (1 - r^2/R^2), warm-up   */
+#define HLBG_IOLET_PULSATILE 2 /* parabolic with umax(t) = peak * (1 - cos(2 pi t/T)) / 2    */
+
+/* site types (Code/geometry/SiteType.h) */
+#define HLBG_SITE_FLUID 1
+#define HLBG_SITE_INLET 2
+#define HLBG_SITE_OUTLET 3
+
+/* link types of the synthetic generator (io/formats/geometry CutType) */
+#define HLBG_LINK_NONE 0
+#define HLBG_LINK_WALL 1
+#define HLBG_LINK_INLET 2
+#define HLBG_LINK_OUTLET 3
+
+/*
+ * Sparse block geometry: the content of a GmyReadResult
+ * (Code/geometry/GmyReadResult.h) restricted to what the LB update reads.
+ * Blocks are 8^3 sites.  A block listed here holds at least one fluid site.
+ * Fluid sites whose links are all fluid-fluid need no record; every fluid site
+ * with a wall or iolet link has one entry in the link_* arrays.
+ * Local site index inside a block: (x * 8 + y) * 8 + z (SiteTraverser order,
+ * Code/geometry/VolumeTraverser.cc:22-52).
+ */
+typedef struct hlbg_geometry {
+  int32_t q;                    /* lattice size; 19 (D3Q19); the oracle also takes 15 */
+  int32_t block_size;           /* must be 8 */
+  int32_t blocks[3];            /* block counts along x, y, z */
+  int64_t n_blocks;             /* number of non-empty blocks */
+  const int32_t *block_coords;  /* [n_blocks*3] block (i,j,k) */
+  const uint64_t *fluid_mask;   /* [n_blocks*8] bit l of word l/64 = site l is fluid */
+  int64_t n_link_sites;         /* fluid sites with at least one wall/iolet link */
+  const int64_t *link_site;     /* [n] block_index*512 + local site index, ascending */
+  const uint32_t *wall_mask;    /* [n] bit d-1 set: link d hits a wall (SiteData) */
+  const uint32_t *iolet_mask;   /* [n] bit d-1 set: link d hits an iolet */
+  const int32_t *iolet_id;      /* [n] iolet index (into the inlet or outlet list), -1 */
+  const int8_t *site_type;      /* [n] HLBG_SITE_* */
+  const float *cut_distance;    /* [n*(q-1)] link fraction to the surface, or NULL */
+  const float *wall_normal;     /* [n*3] or NULL (unused by the update) */
+} hlbg_geometry;
+
+typedef struct hlbg_iolet {
+  int32_t model;       /* HLBG_IOLET_COSINE / PARABOLIC / PULSATILE */
+  int32_t pad_;
+  double position[3];  /* lattice units */
+  double normal[3];    /* normalised on create (InOutLet::SetNormal) */
+  /* pressure (cosine) iolets */
+  double density_mean, density_amp, phase, period;
+  /* velocity iolets */
+  double radius, max_speed, vel_period;
+  uint64_t warmup_steps;
+} hlbg_iolet;
+
+typedef struct hlbg_params {
+  int32_t kernel;     /* HLBG_KERNEL_* */
+  int32_t wall;       /* HLBG_WALL_* */
+  int32_t inlet;      /* HLBG_IOLET_NASH / LADD */
+  int32_t outlet;     /* HLBG_IOLET_NASH / LADD */
+  int32_t precision;  /* HLBG_FP64 / FP32DEV / FP16 */
+  int32_t flags;      /* reserved, 0 */
+  double tau;         /* relaxation time; omega = -1/tau (LbmParameters::CalcDerivedParams) */
+} hlbg_params;
+
+typedef struct hlbg_stats {
+  double mass;             /* sum over sites of density (FP64 accumulation) */
+  double max_du;           /* max over sites |u_new - u_old| (StabilityTester) */
+  double min_f;            /* smallest distribution */
+  int64_t unstable_sites;  /* sites with a distribution <= 0 or NaN */
+  int64_t time_step;       /* 1-indexed SimulationState time step of the next update */
+} hlbg_stats;
+
+typedef struct hlbg_ctx hlbg_ctx;
+
+/* ---- geometry: synthetic generators (seeded, deterministic) ---------------- */
+/* Straight pipe along z, radius R, fluid z in [0, length]; Nash-style inlet at
+ * z=-0.5 (normal +z) and outlet at z=length+0.5 (normal -z). */
+int hlbg_synth_pipe(double radius, int32_t length, int32_t q, int32_t with_cuts,
+                    void **geom_handle);
+/* Bifurcation: parent radius/length, daughters by Murray's law (split ratio s in
+ * [0.3,0.7]), half-angle in [25,60] degrees, seeded. */
+int hlbg_synth_bifurcation(uint64_t seed, double parent_radius, double parent_length,
+                           double daughter_length_factor, int32_t q, int32_t with_cuts,
+                           void **geom_handle);
+/* Stenosed pipe: radius, length, stenosis depth fraction in [0,1). */
+int hlbg_synth_stenosis(double radius, int32_t length, double depth, int32_t q,
+                        int32_t with_cuts, void **geom_handle);
+/* Random vascular forest in a box of box_sites^3 (multiple of 8): n_roots trees
+ * of the given depth, root radius, Murray radii, branch angles in [20,70] deg,
+ * segment length 6-10 x radius. */
+int hlbg_synth_tree(uint64_t seed, int32_t box_sites, int32_t n_roots, int32_t depth,
+                    double root_radius, int32_t q, int32_t with_cuts, int32_t n_threads,
+                    void **geom_handle);
+/* Access the generated geometry and its iolets (pointers stay owned by the handle). */
+int hlbg_synth_view(void *geom_handle, hlbg_geometry *out, int64_t *n_fluid_sites,
+                    int32_t *n_inlets, int32_t *n_outlets);
+int hlbg_synth_iolet(void *geom_handle, int32_t is_outlet, int32_t index, double position[3],
+                     double normal[3], double *radius);
+void hlbg_synth_free(void *geom_handle);
+
+/* ---- solver context -------------------------------------------------------- */
+int hlbg_create(const hlbg_geometry *geom, const hlbg_params *params,
+                const hlbg_iolet *inlets, int32_t n_inlets, const hlbg_iolet *outlets,
+                int32_t n_outlets, hlbg_ctx **out);
+void hlbg_destroy(hlbg_ctx *ctx);
+const char *hlbg_last_error(const hlbg_ctx *ctx);
+
+int64_t hlbg_site_count(const hlbg_ctx *ctx);   /* fluid sites N */
+int64_t hlbg_slot_count(const hlbg_ctx *ctx);   /* device slots (n_blocks * 512) */
+int hlbg_collision_counts(const hlbg_ctx *ctx, int64_t counts[6]);
+size_t hlbg_device_bytes(const hlbg_ctx *ctx);
+
+/* Permutation: ref_to_slot[i] = device slot of contiguous site id i (ref order:
+ * collision type, then Morton block order, then in-block order). */
+int hlbg_site_order(const hlbg_ctx *ctx, int64_t *ref_to_slot);
+
+/* Uniform equilibrium initial condition (both f arrays), time step reset to 1. */
+int hlbg_init_equilibrium(hlbg_ctx *ctx, double density, double vx, double vy, double vz);
+/* Per-site equilibrium start from host fields in contiguous site order
+ * (rho[N], u[N*3]); the learned warm-start hook. */
+int hlbg_init_equilibrium_field(hlbg_ctx *ctx, const double *rho, const double *u);
+
+/* Advance nsteps full time steps on the given CUDA stream (NULL = context stream).
+ * Returns after enqueueing; hlbg_sync waits. */
+int hlbg_step(hlbg_ctx *ctx, int32_t nsteps, void *cuda_stream);
+int hlbg_sync(hlbg_ctx *ctx);
+
+/* Per-range drop-in for one streamer: ranges are contiguous site ids. */
+int hlbg_stream_and_collide_range(hlbg_ctx *ctx, int64_t first, int64_t count);
+int hlbg_post_step_range(hlbg_ctx *ctx, int64_t first, int64_t count);
+int hlbg_swap(hlbg_ctx *ctx); /* SwapOldAndNew + time step increment */
+
+/* Distributions in contiguous site order, AoS [N*q] doubles (FieldData layout).
+ * which = 0: fOld (current), 1: fNew. */
+int hlbg_get_f(hlbg_ctx *ctx, double *host, int32_t which);
+int hlbg_put_f(hlbg_ctx *ctx, const double *host, int32_t which);
+/* Same, device pointers (stream-ordered on the context stream). */
+int hlbg_get_f_device(hlbg_ctx *ctx, double *dev, int32_t which);
+int hlbg_put_f_device(hlbg_ctx *ctx, const double *dev, int32_t which);
+
+/* Density and velocity per site (contiguous order) from the current f. */
+int hlbg_get_macro(hlbg_ctx *ctx, double *rho, double *u);
+
+/* Reductions over the current state (mass, max|du| against the previous call's
+ * velocity, min f, unstable count).  Synchronous. */
+int hlbg_reduce(hlbg_ctx *ctx, hlbg_stats *out);
+
+/* Per-step iolet values the host computed for the steps [t, t+n) (for tests). */
+int hlbg_iolet_density(const hlbg_ctx *ctx, int32_t is_outlet, int32_t index, uint64_t t,
+                       double *density);
+
+/* Measurement helper: enqueue nsteps with hlbg_step and return the elapsed time
+ * between CUDA events recorded on the context stream around them (ms). */
+int hlbg_time_steps(hlbg_ctx *ctx, int32_t nsteps, float *ms);
+
+/* Library build string. */
+const char *hlbg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HEMELB_GB300_H */
