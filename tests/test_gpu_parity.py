@@ -1,0 +1,234 @@
+"""Parity of the CUDA update with the CPU oracle, through the C ABI.
+
+FP64 plain form: bit-exact against the oracle's scalar evaluation order (the
+reference's aarch64 build) and within 1e-12 relative per distribution of the
+SSE3 order (the reference's x86_64 build).  FP32-deviation / FP16-storage forms:
+velocity and pressure error against the FP64 oracle within the stated bounds.
+"""
+import numpy as np
+import pytest
+
+from hemelb_gb300 import capi, cases
+from hemelb_gb300.lbm import LBM, LbmParameters
+from oracle.oracle import ORDER_SCALAR, ORDER_SSE3, OracleLBM
+
+pytestmark = pytest.mark.gpu
+
+THREADS = 8
+
+
+def oracle_for(case, order=ORDER_SCALAR, params=None):
+    o = OracleLBM(case.geometry.view, params or case.params, case.inlets, case.outlets, order=order)
+    o.set_equilibrium()
+    return o
+
+
+def small_bifurcation(**kw):
+    return cases.bifurcation(seed=kw.pop("seed", 11), parent_radius=kw.pop("parent_radius", 8.0),
+                             parent_length=kw.pop("parent_length", 40.0),
+                             daughter_length_factor=kw.pop("daughter_length_factor", 1.2),
+                             period=kw.pop("period", 200.0), **kw)
+
+
+def test_pipe_fp64_bit_exact_full_run():
+    """Straight pipe, 2000 steps from rest: every distribution equal to the oracle."""
+    c = cases.pipe()
+    o = oracle_for(c)
+    o.step(c.steps, THREADS)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(c.steps)
+    f = s.GetFOld()
+    assert f.shape == o.fold().shape
+    assert np.array_equal(f, o.fold())
+    assert np.array_equal(s.GetFNew(), o.fnew())
+
+
+def test_pipe_fp64_within_1e12_of_sse3_order():
+    c = cases.pipe()
+    o = oracle_for(c, ORDER_SSE3)
+    o.step(c.steps, THREADS)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(c.steps)
+    f = s.GetFOld()
+    rel = np.abs(f - o.fold()) / np.abs(o.fold())
+    assert rel.max() <= 1e-12
+
+
+@pytest.mark.parametrize("kernel", [capi.KERNEL_LBGK, capi.KERNEL_TRT])
+def test_bifurcation_bfl_ladd_fp64_bit_exact(kernel):
+    """BFL walls (with PostStep), pulsatile Ladd inlet, Nash outlets, all six types."""
+    c = small_bifurcation()
+    c.params.kernel = kernel
+    counts = None
+    o = oracle_for(c)
+    o.step(400, THREADS)
+    s = c.solver()
+    counts = s.collision_counts
+    assert counts == o.type_count
+    assert all(n > 0 for n in counts), counts
+    s.SetInitialConditions()
+    s.DoTimeStep(400)
+    assert np.array_equal(s.GetFOld(), o.fold())
+    assert np.array_equal(s.GetFNew(), o.fnew())
+
+
+def test_nash_cosine_iolets_with_warmup_bit_exact():
+    """Pulsatile cosine pressure iolets with warm-up from the minimum density."""
+    c = cases.pipe(radius=6.0, length=30)
+    for k, io in enumerate(c.inlets + c.outlets):
+        io.density_amp = 0.002
+        io.period = 50.0
+        io.phase = 0.3 * k
+        io.warmup_steps = 20
+    o = oracle_for(c)
+    o.step(120, THREADS)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(120)
+    assert np.array_equal(s.GetFOld(), o.fold())
+
+
+def test_per_range_streamer_drop_in_matches_oracle():
+    """StreamAndCollide / PostStep over each collision-type range, then swap."""
+    c = small_bifurcation(seed=5)
+    o = oracle_for(c)
+    s = c.solver()
+    s.SetInitialConditions()
+    counts = s.collision_counts
+    for _ in range(3):
+        first = 0
+        for t in range(6):
+            s.StreamAndCollide(first, counts[t])
+            o.stream_and_collide(first, counts[t])
+            first += counts[t]
+        first = 0
+        for t in range(6):
+            s.PostStep(first, counts[t])
+            o.post_step(first, counts[t])
+            first += counts[t]
+        s.SwapOldAndNew()
+        o.swap()
+    assert np.array_equal(s.GetFOld(), o.fold())
+
+
+def test_whole_step_equals_per_range_path():
+    c = small_bifurcation(seed=6)
+    a = c.solver()
+    b = c.solver()
+    a.SetInitialConditions()
+    b.SetInitialConditions()
+    a.DoTimeStep(5)
+    counts = b.collision_counts
+    n = sum(counts)
+    for _ in range(5):
+        b.StreamAndCollide(0, n)
+        b.PostStep(0, n)
+        b.SwapOldAndNew()
+    assert np.array_equal(a.GetFOld(), b.GetFOld())
+
+
+def test_put_get_round_trip_and_continue():
+    """FieldData-layout put/get is exact, and stepping from a put state matches the oracle."""
+    c = small_bifurcation(seed=3)
+    o = oracle_for(c)
+    o.step(7, THREADS)
+    s = c.solver()
+    s.PutF(o.fold(), 0)
+    s.PutF(o.fnew(), 1)
+    assert np.array_equal(s.GetFOld(), o.fold())
+    assert np.array_equal(s.GetFNew(), o.fnew())
+    # the device time step must follow the oracle's 1-indexed step for the iolets
+    s2 = c.solver()
+    s2.SetInitialConditions()
+    s2.DoTimeStep(7)
+    assert np.array_equal(s2.GetFOld(), o.fold())
+    o.step(5, THREADS)
+    s2.DoTimeStep(5)
+    assert np.array_equal(s2.GetFOld(), o.fold())
+
+
+def test_macro_density_velocity_match_oracle():
+    c = cases.pipe(radius=6.0, length=30)
+    o = oracle_for(c)
+    o.step(50, THREADS)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(50)
+    rho, u = s.macro()
+    orho, ou = o.macro()
+    assert np.array_equal(rho, orho)
+    assert np.array_equal(u, ou)
+
+
+def test_reduce_mass_residual_and_instability():
+    c = cases.pipe(radius=6.0, length=30)
+    o = oracle_for(c)
+    o.step(30, THREADS)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(30)
+    st = s.reduce()
+    orho, ou = o.macro(o.f_old)
+    prho, pu = o.macro(o.f_new)
+    assert st.unstable_sites == 0
+    assert abs(st.mass - orho.sum()) <= 1e-9 * orho.sum()
+    du = np.sqrt(((ou - pu) ** 2).sum(axis=1)).max()
+    assert abs(st.max_du - du) <= 1e-15 + 1e-12 * du
+    f = s.GetFOld()
+    f[17, 3] = -1.0e-3
+    f[99, 0] = np.nan
+    s.PutF(f, 0)
+    st = s.reduce()
+    assert st.unstable_sites == 2
+
+
+@pytest.mark.parametrize("precision,u_tol,p_tol", [(capi.FP32DEV, 1e-4, 1e-6), (capi.FP16, 2e-2, 1e-4)])
+def test_precision_forms_error_against_fp64(precision, u_tol, p_tol):
+    """FP32-deviation and FP16-storage forms: relative L2 velocity error and max
+    pressure error (p = rho c_s^2) against the FP64 oracle after 1000 steps."""
+    c = cases.pipe(radius=8.0, length=48)
+    o = oracle_for(c)
+    o.step(1000, THREADS)
+    s = c.solver(precision)
+    s.SetInitialConditions()
+    s.DoTimeStep(1000)
+    rho, u = s.macro()
+    orho, ou = o.macro()
+    u_err = np.linalg.norm(u - ou) / np.linalg.norm(ou)
+    p_err = np.abs(rho - orho).max() / 3.0
+    assert u_err <= u_tol, u_err
+    assert p_err <= p_tol, p_err
+
+
+def test_warm_start_field_init_is_equilibrium():
+    c = cases.pipe(radius=6.0, length=30)
+    s = c.solver()
+    n = s.n_sites
+    rng = np.random.default_rng(0)
+    rho = 1.0 + 1e-3 * rng.standard_normal(n)
+    u = 1e-2 * rng.standard_normal((n, 3))
+    s.SetInitialField(rho, u)
+    f = s.GetFOld()
+    o = oracle_for(c)
+    import ctypes as C
+    feq = np.empty(19)
+    for i in (0, n // 2, n - 1):
+        m = (C.c_double * 3)(*(rho[i] * u[i]))
+        o.lib.hlbo_feq(C.byref(o.p), rho[i], m, feq.ctypes.data_as(C.POINTER(C.c_double)))
+        assert np.array_equal(f[i], feq)
+
+
+def test_invalid_arguments_fail_loudly():
+    c = cases.pipe(radius=4.0, length=10)
+    bad = LbmParameters(tau=0.4)
+    with pytest.raises(capi.HlbgError):
+        LBM(c.geometry, bad, c.inlets, c.outlets)
+    # Ladd streamer with pressure iolets is inconsistent
+    p = LbmParameters(tau=0.8, inlet=capi.IOLET_LADD)
+    with pytest.raises(capi.HlbgError):
+        LBM(c.geometry, p, c.inlets, c.outlets)
+    s = c.solver()
+    with pytest.raises(capi.HlbgError):
+        s.DoTimeStep(1)  # no initial condition yet
