@@ -97,6 +97,7 @@ SIGNATURES = {
     "hlbg_iolet_density": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64,
                                      C.POINTER(C.c_double)]),
     "hlbg_time_steps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
+    "hlbg_time_kernels": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "hlbg_version": (C.c_char_p, []),
 }
 

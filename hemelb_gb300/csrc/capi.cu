@@ -932,6 +932,47 @@ int hlbg_iolet_density(const hlbg_ctx* ctx, int32_t is_outlet, int32_t index, ui
   return HLBG_OK;
 }
 
+int hlbg_time_kernels(hlbg_ctx* ctx, int32_t nsteps, float* collide_ms, float* post_ms) {
+  // Same work as hlbg_step, with CUDA events recorded on the context stream
+  // around every launch; returns the summed device time of each kernel kind.
+  if (!ctx || !collide_ms || !post_ms || nsteps < 0) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  std::vector<cudaEvent_t> ev((size_t)4 * std::max(nsteps, 1));
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  cudaStream_t st = ctx->stream;
+  StepArgs a;
+  int rc = HLBG_OK;
+  for (int k = 0; k < nsteps && !rc; ++k) {
+    if ((k % kStepBatch) == 0) rc = upload_iolet_table(ctx, std::min(kStepBatch, nsteps - k), st);
+    if (rc) break;
+    fill_args(ctx, a);
+    a.iolet_rho = ctx->d_io_tab + (size_t)(k % kStepBatch) * 2 * ctx->n_io;
+    a.iolet_umax = a.iolet_rho + ctx->n_io;
+    cudaEventRecord(ev[4 * k], st);
+    rc = launch_collide(ctx, a, st);
+    cudaEventRecord(ev[4 * k + 1], st);
+    if (!rc) rc = run_post(ctx, st, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps);
+    cudaEventRecord(ev[4 * k + 2], st);
+    ctx->cur ^= 1;
+    ctx->t1++;
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  float c = 0.f, p = 0.f;
+  for (int k = 0; k < nsteps && e == cudaSuccess && !rc; ++k) {
+    float x = 0.f, y = 0.f;
+    cudaEventElapsedTime(&x, ev[4 * k], ev[4 * k + 1]);
+    cudaEventElapsedTime(&y, ev[4 * k + 1], ev[4 * k + 2]);
+    c += x;
+    p += y;
+  }
+  for (auto& ee : ev) cudaEventDestroy(ee);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, cudaGetErrorString(e));
+  *collide_ms = c;
+  *post_ms = p;
+  return HLBG_OK;
+}
+
 int hlbg_time_steps(hlbg_ctx* ctx, int32_t nsteps, float* ms) {
   if (!ctx || !ms) return HLBG_ERR_INVAL;
   CK(cudaStreamSynchronize(ctx->stream));

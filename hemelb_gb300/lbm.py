@@ -242,6 +242,12 @@ class LBM:
         check(self._lib.hlbg_time_steps(self._ctx, n, C.byref(ms)), self._ctx)
         return float(ms.value)
 
+    def time_kernels(self, n: int):
+        c = C.c_float()
+        p = C.c_float()
+        check(self._lib.hlbg_time_kernels(self._ctx, n, C.byref(c), C.byref(p)), self._ctx)
+        return float(c.value), float(p.value)
+
     # ---- FieldData access ------------------------------------------------------
     def GetFOld(self, out: np.ndarray | None = None) -> np.ndarray:
         return self._get_f(0, out)

@@ -217,6 +217,9 @@ int hlbg_iolet_density(const hlbg_ctx *ctx, int32_t is_outlet, int32_t index, ui
 /* Measurement helper: enqueue nsteps with hlbg_step and return the elapsed time
  * between CUDA events recorded on the context stream around them (ms). */
 int hlbg_time_steps(hlbg_ctx *ctx, int32_t nsteps, float *ms);
+/* Same as hlbg_step(nsteps) with events around every launch: summed device time
+ * of the stream-and-collide launches and of the BFL PostStep launches (ms). */
+int hlbg_time_kernels(hlbg_ctx *ctx, int32_t nsteps, float *collide_ms, float *post_ms);
 
 /* Library build string. */
 const char *hlbg_version(void);
