@@ -45,20 +45,26 @@ def _sources_newer(target, sources):
     return any(os.path.getmtime(s) > t for s in sources)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, defines=(), out: str | None = None,
+          build_dir: str | None = None) -> str:
+    """Compile the library (in-tree by default).  `defines` are extra -D flags for
+    the CUDA units (launch-shape knobs); `out` / `build_dir` redirect the output."""
+    lib = out or LIB
+    bdir = build_dir or BUILD
+    os.makedirs(bdir, exist_ok=True)
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [
         os.path.join(HERE, "..", "include", "hemelb_gb300.h")]
-    if not force and not _sources_newer(LIB, deps + [__file__]):
-        return LIB
+    if not force and not _sources_newer(lib, deps + [__file__]):
+        return lib
     jobs = []
     objs = []
     for unit, extra in UNITS:
-        obj = os.path.join(BUILD, unit + ".o")
+        obj = os.path.join(bdir, unit + ".o")
         objs.append(obj)
-        jobs.append([NVCC] + ARCH + COMMON + extra + ["-c", os.path.join(SRC, unit), "-o", obj])
+        jobs.append([NVCC] + ARCH + COMMON + extra + ["-D" + d for d in defines]
+                    + ["-c", os.path.join(SRC, unit), "-o", obj])
     for unit in HOST_UNITS:
-        obj = os.path.join(BUILD, unit + ".o")
+        obj = os.path.join(bdir, unit + ".o")
         objs.append(obj)
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
                      "-I", os.path.join(HERE, "..", "include"), "-c",
@@ -68,10 +74,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

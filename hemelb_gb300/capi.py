@@ -88,6 +88,7 @@ SIGNATURES = {
     "hlbg_stream_and_collide_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "hlbg_post_step_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "hlbg_swap": (C.c_int, [C.c_void_p]),
+    "hlbg_set_time_step": (C.c_int, [C.c_void_p, C.c_uint64]),
     "hlbg_get_f": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
     "hlbg_put_f": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
     "hlbg_get_f_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
@@ -109,7 +110,7 @@ def load(path: str | None = None) -> C.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = path or LIB_PATH
+    p = path or os.environ.get("HEMELB_GB300_LIB") or LIB_PATH
     if not os.path.exists(p):
         raise RuntimeError(
             f"{p} is missing: build it with `python -m hemelb_gb300.build` "

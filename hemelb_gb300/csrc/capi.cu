@@ -28,7 +28,6 @@ using namespace hlbg;
 
 namespace {
 constexpr double kPI = 3.14159265358979323846264338327950288;  // Code/constants.h:18
-constexpr int kMonitorGrid = 152 * 4;
 constexpr int64_t kStageSites = 1 << 22;
 constexpr int kStepBatch = 1024;
 
@@ -597,8 +596,6 @@ int hlbg_create(const hlbg_geometry* g, const hlbg_params* p, const hlbg_iolet* 
     ctx->dev_bytes += bytes;
     CK(cudaMemsetAsync(ctx->f[k], 0, bytes, ctx->stream));
   }
-  if ((rc = dev_alloc(ctx, &ctx->d_part, (size_t)kMonitorGrid * 3))) return rc;
-  if ((rc = dev_alloc(ctx, &ctx->d_part_bad, (size_t)kMonitorGrid))) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   return HLBG_OK;
 }
@@ -780,6 +777,12 @@ int hlbg_swap(hlbg_ctx* ctx) {
   return HLBG_OK;
 }
 
+int hlbg_set_time_step(hlbg_ctx* ctx, uint64_t t1) {
+  if (!ctx || t1 < 1) return HLBG_ERR_INVAL;
+  ctx->t1 = t1;
+  return HLBG_OK;
+}
+
 static int gather_common(hlbg_ctx* ctx, double* out, int32_t which, bool to_host) {
   if (!ctx || !out || (which != 0 && which != 1)) return HLBG_ERR_INVAL;
   int rc = ensure_stage(ctx);
@@ -880,6 +883,12 @@ int hlbg_get_macro(hlbg_ctx* ctx, double* rho, double* u) {
 
 int hlbg_reduce(hlbg_ctx* ctx, hlbg_stats* out) {
   if (!ctx || !out) return HLBG_ERR_INVAL;
+  const int64_t nparts = (ctx->nslot + 255) / 256;
+  if (!ctx->d_part) {
+    int rc = dev_alloc(ctx, &ctx->d_part, (size_t)nparts * 3);
+    if (!rc) rc = dev_alloc(ctx, &ctx->d_part_bad, (size_t)nparts);
+    if (rc) return rc;
+  }
   MonitorArgs ma{};
   ma.f_cur = ctx->f[ctx->cur];
   ma.f_prev = ctx->f[ctx->cur ^ 1];
@@ -888,39 +897,31 @@ int hlbg_reduce(hlbg_ctx* ctx, hlbg_stats* out) {
   ma.site_code = ctx->d_site_code;
   ma.block_bulk = ctx->d_block_bulk;
   ma.part_mass = ctx->d_part;
-  ma.part_max = ctx->d_part + kMonitorGrid;
-  ma.part_min = ctx->d_part + 2 * kMonitorGrid;
+  ma.part_max = ctx->d_part + nparts;
+  ma.part_min = ctx->d_part + 2 * nparts;
   ma.part_bad = ctx->d_part_bad;
   ma.fp16_scale = ctx->fp16_scale;
   ma.fp16_inv_scale = 1.0f / ctx->fp16_scale;
   switch (ctx->prec) {
-    case 0: launch_monitor_0(ma, kMonitorGrid, ctx->stream); break;
-    case 1: launch_monitor_1(ma, kMonitorGrid, ctx->stream); break;
-    default: launch_monitor_2(ma, kMonitorGrid, ctx->stream); break;
+    case 0: launch_monitor_0(ma, 0, ctx->stream); break;
+    case 1: launch_monitor_1(ma, 0, ctx->stream); break;
+    default: launch_monitor_2(ma, 0, ctx->stream); break;
   }
   CK(cudaGetLastError());
-  std::vector<double> part((size_t)kMonitorGrid * 3);
-  std::vector<unsigned long long> bad((size_t)kMonitorGrid);
-  CK(cudaMemcpyAsync(part.data(), ctx->d_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+  double res[3];
+  unsigned long long bad = 0;
+  for (int k = 0; k < 3; ++k)
+    CK(cudaMemcpyAsync(&res[k], ctx->d_part + k * nparts, sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CK(cudaMemcpyAsync(&bad, ctx->d_part_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                      ctx->stream));
-  CK(cudaMemcpyAsync(bad.data(), ctx->d_part_bad, sizeof(unsigned long long) * bad.size(),
-                     cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  double mass = 0.0, mx = 0.0, mn = 1.0e300;
-  int64_t nb = 0;
-  for (int k = 0; k < kMonitorGrid; ++k) {
-    mass += part[k];
-    double m = part[kMonitorGrid + k];
-    if (!(m <= mx)) mx = m;
-    mn = std::min(mn, part[2 * kMonitorGrid + k]);
-    nb += (int64_t)bad[k];
-  }
-  out->mass = mass;
-  out->max_du = mx;
-  out->min_f = mn;
-  out->unstable_sites = nb;
+  out->mass = res[0];
+  out->max_du = res[1];
+  out->min_f = res[2];
+  out->unstable_sites = (int64_t)bad;
   out->time_step = (int64_t)ctx->t1;
-  return nb ? HLBG_ERR_UNSTABLE : HLBG_OK;
+  return bad ? HLBG_ERR_UNSTABLE : HLBG_OK;
 }
 
 int hlbg_iolet_density(const hlbg_ctx* ctx, int32_t is_outlet, int32_t index, uint64_t t,

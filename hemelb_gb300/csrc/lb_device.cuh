@@ -3,7 +3,9 @@
 // Layout in HBM (built by layout.cpp):
 //   * non-empty 8^3 blocks in Morton order; slot = block * 512 + local index,
 //     local = (x * 8 + y) * 8 + z, the reference's SiteTraverser order;
-//   * distributions structure-of-arrays, f[d * stride + slot], two copies
+//   * distributions block-major structure-of-arrays: for block b, direction d and
+//     local site l, f[(b * 19 + d) * 512 + l]; each block's 19 x 512 values are
+//     contiguous, so a site's 19 loads share one base address; two copies
 //     (old / new) swapped every step (FieldData::SwapOldAndNew);
 //   * block_nbr[block * 27 + (dx+1)*9 + (dy+1)*3 + (dz+1)] = neighbouring block
 //     index or -1, staged in shared memory per CTA;
@@ -127,6 +129,11 @@ struct Store<2> {
     p[i] = __float2half_rn(v * a.fp16_scale);
   }
 };
+
+// Element index of (slot s, direction d) in the block-major layout.
+__host__ __device__ __forceinline__ int64_t fidx(int64_t s, int d) {
+  return ((s >> 9) * Q + d) * kSites + (s & (kSites - 1));
+}
 
 __device__ __forceinline__ int bit(uint32_t m, int d) { return d ? (int)((m >> (d - 1)) & 1u) : 0; }
 

@@ -5,145 +5,201 @@
 #include "lb_device.cuh"
 #include "lb_launch.h"
 
+// Launch shape of the stream-and-collide kernel (threads per CTA must divide 512;
+// minimum resident CTAs per SM for the FP32 / FP16 forms and for FP64).
+#ifndef HLBG_SC_THREADS
+#define HLBG_SC_THREADS 256
+#endif
+#ifndef HLBG_SC_MINB
+#define HLBG_SC_MINB 4
+#endif
+#ifndef HLBG_SC_MINB64
+#define HLBG_SC_MINB64 2
+#endif
+
 namespace hlbg {
+
+template <int P>
+struct Calc {
+  using T = float;
+};
+template <>
+struct Calc<0> {
+  using T = double;
+};
+
+// ---------------------------------------------------------------------------
+// Value an iolet link writes into the site's own inverse-direction slot:
+// Nash (NashZerothOrderPressure.h:388-421) or Ladd (LaddIolet.h:465-502).  Out of
+// line with scalar arguments: iolet links are a fraction of a percent of links.
+// m0 is the density (FP64 form) or the density deviation (FP32 / FP16 forms).
+// ---------------------------------------------------------------------------
+template <int P>
+__device__ __noinline__ typename Calc<P>::T iolet_link_value(
+    const StepArgs& a, int gi, int model, int d, typename Calc<P>::T fpost_d,
+    typename Calc<P>::T m0, typename Calc<P>::T mx, typename Calc<P>::T my,
+    typename Calc<P>::T mz, int gx, int gy, int gz) {
+  using T = typename Calc<P>::T;
+  const int un = c_inv[d];
+  const IoletDev& io = a.iolets[gi];
+  if (model == 0) {
+    if constexpr (P == 0) {
+      return nash64(io, a.iolet_rho[gi], m0, mx, my, mz, un);
+    } else {
+      const double grho = a.iolet_rho[gi];
+      const float gdr = (float)(grho - 1.0);
+      const float grho_f = (float)grho;
+      const float rho = 1.f + m0;
+      const float comp = (mx * (float)io.nf[0] + my * (float)io.nf[1] + mz * (float)io.nf[2]) / rho;
+      const float gxv = (float)io.nf[0] * comp * grho_f;
+      const float gyv = (float)io.nf[1] * comp * grho_f;
+      const float gzv = (float)io.nf[2] * comp * grho_f;
+      const float inv_g = 1.f / grho_f;
+      const float mde = c_cx[un] * gxv + c_cy[un] * gyv + c_cz[un] * gzv;
+      return (float)weight_d(un) *
+             ((gdr - 1.5f * (gxv * gxv + gyv * gyv + gzv * gzv) * inv_g) + mde * (3.f + 4.5f * inv_g * mde));
+    }
+  }
+  const double rho = (P == 0) ? (double)m0 : 1.0 + (double)m0;
+  return fpost_d - (T)ladd_correction64(io, a.iolet_umax[gi], rho, gx, gy, gz, d);
+}
+
+// Per-link dispatch of a site next to a wall or an iolet, unrolled over the 19
+// directions (StreamerTypeFactory.h:65-79: iolet first, then wall, else bulk).
+template <int P, int D>
+struct BoundaryAll {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, int64_t s,
+                                             int x, int y, int z, uint32_t wm, uint32_t im,
+                                             int type, int ioid, int64_t r, const T* fpost, T m0,
+                                             T mx, T my, T mz, const int32_t* block_xyz) {
+    constexpr int inv = Lat::inv(D);
+    const int64_t own = fidx(s, 0) - (int64_t)(s & (kSites - 1));  // this block's element base
+    const int l = (int)(s & (kSites - 1));
+    if (D > 0 && type >= 2 && ((im >> (D - 1)) & 1u)) {
+      const bool is_inlet = (type == 2 || type == 4);
+      const int gi = is_inlet ? ioid : a.n_in + ioid;
+      const int model = is_inlet ? a.inlet_model : a.outlet_model;
+      const int64_t b = s >> 9;
+      const T v = iolet_link_value<P>(a, gi, model, D, fpost[D], m0, mx, my, mz,
+                                      block_xyz[3 * b] * 8 + x, block_xyz[3 * b + 1] * 8 + y,
+                                      block_xyz[3 * b + 2] * 8 + z);
+      Store<P>::store(fn + own, inv * kSites + l, v, a);
+    } else if (D > 0 && (type == 1 || type == 4 || type == 5) && ((wm >> (D - 1)) & 1u)) {
+      T v = fpost[D];
+      if (a.wall == 1) {
+        const T q = (T)a.b_cut[r * (Q - 1) + D - 1];
+        if (!(((wm >> (inv - 1)) & 1u) || q < (T)0.5))
+          v = (fpost[D] + ((T)2.0 * q - (T)1) * fpost[inv]) / ((T)2.0 * q);
+      }
+      Store<P>::store(fn + own, inv * kSites + l, v, a);
+    } else {
+      constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
+      const int xx = x + cx, yy = y + cy, zz = z + cz;
+      const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
+      const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+      const int64_t nbase = base(k);
+      if (nbase >= 0) {
+        const int64_t ns = nbase / Q + tl;  // neighbour slot (block * 512 + local)
+        const uint32_t nc = a.block_bulk[ns >> 9] ? 1u : a.site_code[ns];
+        if (nc != 0) Store<P>::store(fn + nbase, D * kSites + tl, fpost[D], a);
+      }
+    }
+    BoundaryAll<P, D + 1>::run(fn, a, base, s, x, y, z, wm, im, type, ioid, r, fpost, m0, mx, my, mz,
+                               block_xyz);
+  }
+};
+template <int P>
+struct BoundaryAll<P, Q> {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int64_t, int, int, int,
+                                             uint32_t, uint32_t, int, int, int64_t, const T*, T, T, T,
+                                             T, const int32_t*) {}
+};
+
+// Element offset (block * 19 * 512) of the 27 blocks around a site's block: from
+// shared memory in the all-slots kernel, from the global table in the list kernel.
+struct SmemBase {
+  const int64_t* sh;
+  __device__ __forceinline__ int64_t operator()(int k) const { return sh[k]; }
+};
+struct GlobalBase {
+  const int32_t* tab;
+  __device__ __forceinline__ int64_t operator()(int k) const {
+    const int32_t nb = __ldg(tab + k);
+    return nb < 0 ? (int64_t)-1 : (int64_t)nb * (Q * kSites);
+  }
+};
+
+// Push of a bulk site's post-collision value along direction D (compile-time):
+// neighbour block from the 27-entry table, local index by wrap-around arithmetic.
+template <int P, int D>
+struct PushAll {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, int x, int y,
+                                             int z, const T* fpost) {
+    constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
+    const int xx = x + cx, yy = y + cy, zz = z + cz;
+    const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
+    const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+    Store<P>::store(fn + base(k), D * kSites + tl, fpost[D], a);
+    PushAll<P, D + 1>::run(fn, a, base, x, y, z, fpost);
+  }
+};
+template <int P>
+struct PushAll<P, Q> {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int, int, int, const T*) {}
+};
 
 // ---------------------------------------------------------------------------
 // One site: collide, then push along the 19 links.
 // ---------------------------------------------------------------------------
-template <int P>
-__device__ __forceinline__ void site_update(const StepArgs& a, const int32_t* nbr, int64_t s,
-                                            uint32_t code, const int32_t* block_xyz) {
+template <int P, class B>
+__device__ __forceinline__ void site_update(const StepArgs& a, const B& base,
+                                            const int32_t* __restrict__ tab, int64_t s,
+                                            uint32_t code, const int32_t* __restrict__ block_xyz) {
   using St = Store<P>;
   using S = typename St::S;
-  const S* fo = static_cast<const S*>(a.f_old);
-  S* fn = static_cast<S*>(a.f_new);
+  using T = typename Calc<P>::T;
   const int l = (int)(s & (kSites - 1));
-  if constexpr (P == 0) {
-    double f[Q], fpost[Q];
+  const int64_t b = s >> 9;
+  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + l;
+  S* fn = static_cast<S*>(a.f_new);
+  T f[Q], fpost[Q];
 #pragma unroll
-    for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * a.stride + s, a);
-    double rho, mx, my, mz;
-    collide64(a, f, rho, mx, my, mz, fpost);
-    if (code == 1) {
-#pragma unroll
-      for (int i = 0; i < Q; ++i) St::store(fn, i * a.stride + nbr_slot(nbr, l, i), fpost[i], a);
-      return;
-    }
-    const int64_t r = code - 2;
-    const uint32_t wm = a.b_wall[r], im = a.b_iolet[r];
-    const int type = a.b_type[r];
-    const int ioid = a.b_ioid[r];
-    const bool can_wall = (type == 1 || type == 4 || type == 5);
-    const bool can_iolet = type >= 2;
-    const bool is_inlet = (type == 2 || type == 4);
-#pragma unroll
-    for (int d = 0; d < Q; ++d) {
-      if (can_iolet && bit(im, d)) {
-        const int gi = is_inlet ? ioid : a.n_in + ioid;
-        const int model = is_inlet ? a.inlet_model : a.outlet_model;
-        const int un = Lat::inv(d);
-        double v;
-        if (model == 0) {
-          v = nash64(a.iolets[gi], a.iolet_rho[gi], rho, mx, my, mz, un);
-        } else {
-          const int64_t b = s >> 9;
-          const int gx = block_xyz[3 * b] * 8 + (l >> 6);
-          const int gy = block_xyz[3 * b + 1] * 8 + ((l >> 3) & 7);
-          const int gz = block_xyz[3 * b + 2] * 8 + (l & 7);
-          v = fpost[d] - ladd_correction64(a.iolets[gi], a.iolet_umax[gi], rho, gx, gy, gz, d);
-        }
-        St::store(fn, un * a.stride + s, v, a);
-      } else if (can_wall && bit(wm, d)) {
-        const int inv = Lat::inv(d);
-        double v = fpost[d];
-        if (a.wall == 1) {
-          const double q = (double)a.b_cut[r * (Q - 1) + d - 1];
-          if (!(bit(wm, inv) || q < 0.5)) v = (fpost[d] + (2.0 * q - 1) * fpost[inv]) / (2.0 * q);
-        }
-        St::store(fn, inv * a.stride + s, v, a);
-      } else {
-        const int64_t ns = nbr_slot(nbr, l, d);
-        if (ns < 0) continue;
-        const uint32_t nc = a.block_bulk[ns >> 9] ? 1u : a.site_code[ns];
-        if (nc == 0) continue;  // rubbish site
-        St::store(fn, d * a.stride + ns, fpost[d], a);
-      }
-    }
-  } else {
-    float g[Q], gpost[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) g[i] = St::load(fo, i * a.stride + s, a);
-    float dr, mx, my, mz;
-    collide_dev(a, g, dr, mx, my, mz, gpost);
-    if (code == 1) {
-#pragma unroll
-      for (int i = 0; i < Q; ++i) St::store(fn, i * a.stride + nbr_slot(nbr, l, i), gpost[i], a);
-      return;
-    }
-    const int64_t r = code - 2;
-    const uint32_t wm = a.b_wall[r], im = a.b_iolet[r];
-    const int type = a.b_type[r];
-    const int ioid = a.b_ioid[r];
-    const bool can_wall = (type == 1 || type == 4 || type == 5);
-    const bool can_iolet = type >= 2;
-    const bool is_inlet = (type == 2 || type == 4);
-    const float rho = 1.f + dr;
-#pragma unroll
-    for (int d = 0; d < Q; ++d) {
-      if (can_iolet && bit(im, d)) {
-        const int gi = is_inlet ? ioid : a.n_in + ioid;
-        const int model = is_inlet ? a.inlet_model : a.outlet_model;
-        const int un = Lat::inv(d);
-        float v;
-        const IoletDev& io = a.iolets[gi];
-        if (model == 0) {
-          const double grho = a.iolet_rho[gi];
-          const float gdr = (float)(grho - 1.0);
-          const float grho_f = (float)grho;
-          const float comp = (mx * (float)io.nf[0] + my * (float)io.nf[1] + mz * (float)io.nf[2]) / rho;
-          const float gx = (float)io.nf[0] * comp * grho_f;
-          const float gy = (float)io.nf[1] * comp * grho_f;
-          const float gz = (float)io.nf[2] * comp * grho_f;
-          const float inv_g = 1.f / grho_f;
-          v = geq_dev(gdr, inv_g, 1.5f * (gx * gx + gy * gy + gz * gz), gx, gy, gz, un);
-        } else {
-          const int64_t b = s >> 9;
-          const int gxx = block_xyz[3 * b] * 8 + (l >> 6);
-          const int gyy = block_xyz[3 * b + 1] * 8 + ((l >> 3) & 7);
-          const int gzz = block_xyz[3 * b + 2] * 8 + (l & 7);
-          v = gpost[d] - (float)ladd_correction64(io, a.iolet_umax[gi], (double)rho, gxx, gyy, gzz, d);
-        }
-        St::store(fn, un * a.stride + s, v, a);
-      } else if (can_wall && bit(wm, d)) {
-        const int inv = Lat::inv(d);
-        float v = gpost[d];
-        if (a.wall == 1) {
-          const float q = a.b_cut[r * (Q - 1) + d - 1];
-          if (!(bit(wm, inv) || q < 0.5f)) v = (gpost[d] + (2.f * q - 1.f) * gpost[inv]) / (2.f * q);
-        }
-        St::store(fn, inv * a.stride + s, v, a);
-      } else {
-        const int64_t ns = nbr_slot(nbr, l, d);
-        if (ns < 0) continue;
-        const uint32_t nc = a.block_bulk[ns >> 9] ? 1u : a.site_code[ns];
-        if (nc == 0) continue;
-        St::store(fn, d * a.stride + ns, gpost[d], a);
-      }
-    }
+  for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
+  T m0, mx, my, mz;
+  if constexpr (P == 0)
+    collide64(a, f, m0, mx, my, mz, fpost);
+  else
+    collide_dev(a, f, m0, mx, my, mz, fpost);
+  if (code == 1) {
+    PushAll<P, 0>::run(fn, a, base, l >> 6, (l >> 3) & 7, l & 7, fpost);
+    return;
   }
+  const int64_t r = code - 2;
+  BoundaryAll<P, 0>::run(fn, a, base, s, l >> 6, (l >> 3) & 7, l & 7, a.b_wall[r], a.b_iolet[r],
+                         (int)a.b_type[r], a.b_ioid[r], r, fpost, m0, mx, my, mz, block_xyz);
 }
 
 template <int P>
-__global__ void __launch_bounds__(256) k_stream_collide(StepArgs a, const int32_t* block_xyz) {
-  __shared__ int32_t sh_nbr[27];
-  const int64_t s = (int64_t)blockIdx.x * 256 + threadIdx.x;
-  const int64_t b = ((int64_t)blockIdx.x * 256) >> 9;
-  if (threadIdx.x < 27) sh_nbr[threadIdx.x] = a.block_nbr[b * 27 + threadIdx.x];
+__global__ void __launch_bounds__(HLBG_SC_THREADS, (P == 0 ? HLBG_SC_MINB64 : HLBG_SC_MINB))
+    k_stream_collide(StepArgs a, const int32_t* block_xyz) {
+  __shared__ int64_t sh_base[27];
+  const int64_t s0 = (int64_t)blockIdx.x * HLBG_SC_THREADS;
+  const int64_t b = s0 >> 9;
+  const int32_t* tab = a.block_nbr + b * 27;
+  if (threadIdx.x < 27) {
+    const int32_t nb = tab[threadIdx.x];
+    sh_base[threadIdx.x] = nb < 0 ? (int64_t)-1 : (int64_t)nb * (Q * kSites);
+  }
   __syncthreads();
+  const int64_t s = s0 + threadIdx.x;
   if (s >= a.nslot) return;
   const uint32_t code = a.block_bulk[b] ? 1u : a.site_code[s];
   if (code == 0) return;
-  site_update<P>(a, sh_nbr, s, code, block_xyz);
+  site_update<P>(a, SmemBase{sh_base}, tab, s, code, block_xyz);
 }
 
 template <int P>
@@ -154,7 +210,8 @@ __global__ void __launch_bounds__(256) k_stream_collide_list(StepArgs a, const i
   const int64_t b = s >> 9;
   const uint32_t code = a.block_bulk[b] ? 1u : a.site_code[s];
   if (code == 0) return;
-  site_update<P>(a, a.block_nbr + b * 27, s, code, block_xyz);
+  const int32_t* tab = a.block_nbr + b * 27;
+  site_update<P>(a, GlobalBase{tab}, tab, s, code, block_xyz);
 }
 
 // BouzidiFirdaousLallemandLink::PostStepLink (BouzidiFirdaousLallemand.h:336-357)
@@ -174,14 +231,14 @@ __global__ void k_post_step(PostArgs p) {
   const int inv = c_inv[d];
   if constexpr (P == 0) {
     const double q = (double)p.q[i];
-    const double vi = St::load(fn, inv * p.stride + s, a);
-    const double vd = St::load(fn, d * p.stride + s, a);
-    St::store(fn, inv * p.stride + s, 2.0 * q * vi + (1.0 - 2.0 * q) * vd, a);
+    const double vi = St::load(fn, fidx(s, inv), a);
+    const double vd = St::load(fn, fidx(s, d), a);
+    St::store(fn, fidx(s, inv), 2.0 * q * vi + (1.0 - 2.0 * q) * vd, a);
   } else {
     const float q = p.q[i];
-    const float vi = St::load(fn, inv * p.stride + s, a);
-    const float vd = St::load(fn, d * p.stride + s, a);
-    St::store(fn, inv * p.stride + s, 2.f * q * vi + (1.f - 2.f * q) * vd, a);
+    const float vi = St::load(fn, fidx(s, inv), a);
+    const float vd = St::load(fn, fidx(s, d), a);
+    St::store(fn, fidx(s, inv), 2.f * q * vi + (1.f - 2.f * q) * vd, a);
   }
 }
 
@@ -202,11 +259,11 @@ __global__ void k_init_uniform(InitArgs ia) {
 #pragma unroll
   for (int d = 0; d < Q; ++d) {
     if constexpr (P == 0) {
-      St::store(f0, d * ia.stride + s, ia.value[d], a);
-      St::store(f1, d * ia.stride + s, ia.value[d], a);
+      St::store(f0, fidx(s, d), ia.value[d], a);
+      St::store(f1, fidx(s, d), ia.value[d], a);
     } else {
-      St::store(f0, d * ia.stride + s, (float)ia.value[d], a);
-      St::store(f1, d * ia.stride + s, (float)ia.value[d], a);
+      St::store(f0, fidx(s, d), (float)ia.value[d], a);
+      St::store(f1, fidx(s, d), (float)ia.value[d], a);
     }
   }
 }
@@ -231,12 +288,12 @@ __global__ void k_init_field(FieldArgs fa) {
 #pragma unroll
   for (int d = 0; d < Q; ++d) {
     if constexpr (P == 0) {
-      St::store(f0, d * fa.stride + s, feq[d], a);
-      St::store(f1, d * fa.stride + s, feq[d], a);
+      St::store(f0, fidx(s, d), feq[d], a);
+      St::store(f1, fidx(s, d), feq[d], a);
     } else {
       const float v = (float)(feq[d] - weight_d(d));
-      St::store(f0, d * fa.stride + s, v, a);
-      St::store(f1, d * fa.stride + s, v, a);
+      St::store(f0, fidx(s, d), v, a);
+      St::store(f1, fidx(s, d), v, a);
     }
   }
 }
@@ -255,7 +312,7 @@ __global__ void k_gather(GatherArgs ga) {
   const S* f = static_cast<const S*>(ga.f);
 #pragma unroll
   for (int d = 0; d < Q; ++d) {
-    double v = (double)St::load(f, d * ga.stride + s, a);
+    double v = (double)St::load(f, fidx(s, d), a);
     if constexpr (P != 0) v += weight_d(d);
     ga.aos[i * Q + d] = v;
   }
@@ -276,9 +333,9 @@ __global__ void k_scatter(GatherArgs ga) {
   for (int d = 0; d < Q; ++d) {
     const double v = ga.aos[i * Q + d];
     if constexpr (P == 0)
-      St::store(f, d * ga.stride + s, v, a);
+      St::store(f, fidx(s, d), v, a);
     else
-      St::store(f, d * ga.stride + s, (float)(v - weight_d(d)), a);
+      St::store(f, fidx(s, d), (float)(v - weight_d(d)), a);
   }
 }
 
@@ -298,7 +355,7 @@ __global__ void k_macro(GatherArgs ga) {
     double r = 0.0, x = 0.0, y = 0.0, z = 0.0;
 #pragma unroll
     for (int d = 0; d < Q; ++d) {
-      const double v = St::load(f, d * ga.stride + s, a);
+      const double v = St::load(f, fidx(s, d), a);
       r += v;
       x += (double)Lat::cx(d) * v;
       y += (double)Lat::cy(d) * v;
@@ -311,7 +368,7 @@ __global__ void k_macro(GatherArgs ga) {
   } else {
     float g[Q];
 #pragma unroll
-    for (int d = 0; d < Q; ++d) g[d] = St::load(f, d * ga.stride + s, a);
+    for (int d = 0; d < Q; ++d) g[d] = St::load(f, fidx(s, d), a);
     float dr, mx, my, mz;
     moments_dev(g, dr, mx, my, mz);
     const double rho = 1.0 + (double)dr;
@@ -323,8 +380,43 @@ __global__ void k_macro(GatherArgs ga) {
 }
 
 // StabilityTester::PostSendToParent (Code/lb/StabilityTester.h:91-149) and
-// ComputeRelativeDifference (:160-183) over all fluid slots, plus total mass.
-// Fixed grid, one partial per CTA: the host sums the partials in a fixed order.
+// ComputeRelativeDifference (:160-183) plus total mass: one slot per thread, one
+// partial per CTA, reduced by k_monitor_final in a fixed order (deterministic).
+struct MonAcc {
+  double mass, maxdu, minf;
+  unsigned long long bad;
+};
+
+__device__ __forceinline__ void mon_combine(MonAcc& a, const MonAcc& b) {
+  a.mass += b.mass;
+  if (!(b.maxdu <= a.maxdu)) a.maxdu = b.maxdu;  // NaN-propagating max
+  a.minf = fmin(a.minf, b.minf);
+  a.bad += b.bad;
+}
+
+__device__ __forceinline__ MonAcc mon_shfl(const MonAcc& v, int off) {
+  MonAcc o;
+  o.mass = __shfl_down_sync(0xffffffffu, v.mass, off);
+  o.maxdu = __shfl_down_sync(0xffffffffu, v.maxdu, off);
+  o.minf = __shfl_down_sync(0xffffffffu, v.minf, off);
+  o.bad = __shfl_down_sync(0xffffffffu, v.bad, off);
+  return o;
+}
+
+// CTA-wide reduction (256 threads) in a fixed order; result valid in thread 0.
+__device__ __forceinline__ MonAcc mon_block(MonAcc v) {
+  __shared__ MonAcc sh[8];
+  for (int off = 16; off > 0; off >>= 1) mon_combine(v, mon_shfl(v, off));
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : MonAcc{0.0, 0.0, 1.0e300, 0ull};
+    for (int off = 4; off > 0; off >>= 1) mon_combine(v, mon_shfl(v, off));
+  }
+  return v;
+}
+
 template <int P>
 __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
   using St = Store<P>;
@@ -332,64 +424,85 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
   StepArgs a{};
   a.fp16_scale = ma.fp16_scale;
   a.fp16_inv_scale = ma.fp16_inv_scale;
-  const S* fc = static_cast<const S*>(ma.f_cur);
-  const S* fp = static_cast<const S*>(ma.f_prev);
-  double mass = 0.0, maxdu = 0.0, minf = 1.0e300;
-  unsigned long long unstable = 0;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ma.nslot;
-       s += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t code = ma.block_bulk[s >> 9] ? 1u : ma.site_code[s];
-    if (code == 0) continue;
-    double rn = 0.0, xn = 0.0, yn = 0.0, zn = 0.0, ro = 0.0, xo = 0.0, yo = 0.0, zo = 0.0;
+  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t code = (s < ma.nslot) ? (ma.block_bulk[s >> 9] ? 1u : ma.site_code[s]) : 0u;
+  if (code != 0) {
+    const int64_t off = fidx(s, 0);
+    const S* fc = static_cast<const S*>(ma.f_cur) + off;
+    const S* fp = static_cast<const S*>(ma.f_prev) + off;
     bool bad = false;
+    double rn, dx, dy, dz;
+    if constexpr (P == 0) {
+      // Lattice::CalculateDensityAndMomentum (scalar order) on fNew and fOld
+      double xn = 0.0, yn = 0.0, zn = 0.0, ro = 0.0, xo = 0.0, yo = 0.0, zo = 0.0;
+      rn = 0.0;
 #pragma unroll
-    for (int d = 0; d < Q; ++d) {
-      double vn = (double)St::load(fc, d * ma.stride + s, a);
-      double vo = (double)St::load(fp, d * ma.stride + s, a);
-      if constexpr (P != 0) {
-        vn += weight_d(d);
-        vo += weight_d(d);
+      for (int d = 0; d < Q; ++d) {
+        const double vn = St::load(fc, d * kSites, a);
+        const double vo = St::load(fp, d * kSites, a);
+        if (!(vn > 0.0)) bad = true;
+        acc.minf = fmin(acc.minf, vn);
+        rn += vn;
+        xn += (double)Lat::cx(d) * vn;
+        yn += (double)Lat::cy(d) * vn;
+        zn += (double)Lat::cz(d) * vn;
+        ro += vo;
+        xo += (double)Lat::cx(d) * vo;
+        yo += (double)Lat::cy(d) * vo;
+        zo += (double)Lat::cz(d) * vo;
       }
-      if (!(vn > 0.0)) bad = true;
-      minf = fmin(minf, vn);
-      rn += vn;
-      xn += (double)Lat::cx(d) * vn;
-      yn += (double)Lat::cy(d) * vn;
-      zn += (double)Lat::cz(d) * vn;
-      ro += vo;
-      xo += (double)Lat::cx(d) * vo;
-      yo += (double)Lat::cy(d) * vo;
-      zo += (double)Lat::cz(d) * vo;
+      dx = xn / rn - xo / ro;
+      dy = yn / rn - yo / ro;
+      dz = zn / rn - zo / ro;
+    } else {
+      // deviation form: moments in FP32 on g = f - w, the rest in FP64
+      float gn[Q], go[Q];
+      float mn = 1.0e30f;
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        gn[d] = St::load(fc, d * kSites, a);
+        go[d] = St::load(fp, d * kSites, a);
+        const float fv = gn[d] + weight_f(d);
+        if (!(fv > 0.f)) bad = true;
+        mn = fminf(mn, fv);
+      }
+      acc.minf = (double)mn;
+      float drn, mxn, myn, mzn, dro, mxo, myo, mzo;
+      moments_dev(gn, drn, mxn, myn, mzn);
+      moments_dev(go, dro, mxo, myo, mzo);
+      rn = 1.0 + (double)drn;
+      const double ro = 1.0 + (double)dro;
+      dx = (double)mxn / rn - (double)mxo / ro;
+      dy = (double)myn / rn - (double)myo / ro;
+      dz = (double)mzn / rn - (double)mzo / ro;
     }
-    if (bad) unstable++;
-    mass += rn;
-    const double dx = xn / rn - xo / ro, dy = yn / rn - yo / ro, dz = zn / rn - zo / ro;
-    const double du = sqrt(dot3d(dx, dy, dz, dx, dy, dz));
-    if (!(du <= maxdu)) maxdu = du;  // NaN-propagating max
+    acc.bad = bad ? 1ull : 0ull;
+    acc.mass = rn;
+    acc.maxdu = sqrt(dot3d(dx, dy, dz, dx, dy, dz));
   }
-  // block reduction
-  __shared__ double sh_mass[256], sh_max[256], sh_min[256];
-  __shared__ unsigned long long sh_bad[256];
-  sh_mass[threadIdx.x] = mass;
-  sh_max[threadIdx.x] = maxdu;
-  sh_min[threadIdx.x] = minf;
-  sh_bad[threadIdx.x] = unstable;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (threadIdx.x < w) {
-      sh_mass[threadIdx.x] += sh_mass[threadIdx.x + w];
-      const double m2 = sh_max[threadIdx.x + w];
-      if (!(m2 <= sh_max[threadIdx.x])) sh_max[threadIdx.x] = m2;
-      sh_min[threadIdx.x] = fmin(sh_min[threadIdx.x], sh_min[threadIdx.x + w]);
-      sh_bad[threadIdx.x] += sh_bad[threadIdx.x + w];
-    }
-    __syncthreads();
-  }
+  acc = mon_block(acc);
   if (threadIdx.x == 0) {
-    ma.part_mass[blockIdx.x] = sh_mass[0];
-    ma.part_max[blockIdx.x] = sh_max[0];
-    ma.part_min[blockIdx.x] = sh_min[0];
-    ma.part_bad[blockIdx.x] = sh_bad[0];
+    ma.part_mass[blockIdx.x] = acc.mass;
+    ma.part_max[blockIdx.x] = acc.maxdu;
+    ma.part_min[blockIdx.x] = acc.minf;
+    ma.part_bad[blockIdx.x] = acc.bad;
+  }
+}
+
+// Reduce the per-CTA partials of k_monitor in a fixed order into element 0 of
+// each partial array (one CTA of 256 threads; thread t folds partials t, t+256, ...).
+static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, int64_t nparts) {
+  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  for (int64_t i = threadIdx.x; i < nparts; i += blockDim.x)
+    mon_combine(acc, MonAcc{ma.part_mass[i], ma.part_max[i], ma.part_min[i], ma.part_bad[i]});
+  __syncthreads();
+  acc = mon_block(acc);
+  if (threadIdx.x == 0) {
+    ma.part_mass[0] = acc.mass;
+    ma.part_max[0] = acc.maxdu;
+    ma.part_min[0] = acc.minf;
+    ma.part_bad[0] = acc.bad;
   }
 }
 
@@ -402,8 +515,8 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
       unsigned g = (unsigned)((a.list_count + 255) / 256);                                      \
       if (g) k_stream_collide_list<P><<<g, 256, 0, st>>>(a, bxyz);                              \
     } else {                                                                                    \
-      unsigned g = (unsigned)((a.nslot + 255) / 256);                                           \
-      if (g) k_stream_collide<P><<<g, 256, 0, st>>>(a, bxyz);                                   \
+      unsigned g = (unsigned)((a.nslot + HLBG_SC_THREADS - 1) / HLBG_SC_THREADS);               \
+      if (g) k_stream_collide<P><<<g, HLBG_SC_THREADS, 0, st>>>(a, bxyz);                       \
     }                                                                                           \
   }                                                                                             \
   void launch_post_step_##P(const PostArgs& p, cudaStream_t st) {                               \
@@ -431,6 +544,9 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
     if (g) k_macro<P><<<g, 256, 0, st>>>(ga);                                                   \
   }                                                                                             \
   void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st) {                   \
-    k_monitor<P><<<grid, 256, 0, st>>>(ma);                                                     \
+    (void)grid;                                                                                 \
+    const int64_t nparts = (ma.nslot + 255) / 256;                                              \
+    k_monitor<P><<<(unsigned)nparts, 256, 0, st>>>(ma);                                         \
+    k_monitor_final<<<1, 256, 0, st>>>(ma, nparts);                                             \
   }                                                                                             \
   }

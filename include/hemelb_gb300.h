@@ -194,6 +194,9 @@ int hlbg_sync(hlbg_ctx *ctx);
 int hlbg_stream_and_collide_range(hlbg_ctx *ctx, int64_t first, int64_t count);
 int hlbg_post_step_range(hlbg_ctx *ctx, int64_t first, int64_t count);
 int hlbg_swap(hlbg_ctx *ctx); /* SwapOldAndNew + time step increment */
+/* Set the 1-indexed time step of the next update (SimulationState::GetTimeStep;
+ * Code/lb/SimulationState.cc:40-48), e.g. after loading a checkpoint. */
+int hlbg_set_time_step(hlbg_ctx *ctx, uint64_t t1);
 
 /* Distributions in contiguous site order, AoS [N*q] doubles (FieldData layout).
  * which = 0: fOld (current), 1: fNew. */
