@@ -322,7 +322,7 @@ def main():
         cpu = {"value": cn * ck / cdt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
                "sample": "%d fluid sites (first Morton-ordered blocks of the same geometry), %d steps, "
                          "FP64 oracle, scalar order, OpenMP" % (cn, ck)}
-    launches = args.steps * (1 + (1 if lbm.params.wall == capi.WALL_BFL else 0))
+    launches = args.steps * int(lbm._lib.hlbg_launches_per_step(lbm.ctx))
     cfg.update({"fluid_sites": int(n), "slots": int(lbm.n_slots),
                 "collision_counts": list(lbm.collision_counts), "device_bytes": lbm.device_bytes(),
                 "l2": "inputs (distribution arrays) far larger than L2; no flush",

@@ -78,6 +78,7 @@ SIGNATURES = {
     "hlbg_last_error": (C.c_char_p, [C.c_void_p]),
     "hlbg_site_count": (C.c_int64, [C.c_void_p]),
     "hlbg_slot_count": (C.c_int64, [C.c_void_p]),
+    "hlbg_launches_per_step": (C.c_int32, [C.c_void_p]),
     "hlbg_collision_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "hlbg_device_bytes": (C.c_size_t, [C.c_void_p]),
     "hlbg_site_order": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),

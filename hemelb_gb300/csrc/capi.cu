@@ -104,6 +104,10 @@ struct hlbg_ctx {
   int32_t* d_b_ioid = nullptr;
   int8_t* d_b_type = nullptr;
   float* d_b_cut = nullptr;
+  uint64_t* d_b_links = nullptr;  // 3-bit link code per direction (see lb_device.cuh)
+  int32_t* d_rec_slot = nullptr;  // slot of each record
+  int32_t* d_io_rec = nullptr;    // records with at least one iolet link
+  int64_t n_io_rec = 0;
   int32_t* d_ref2slot = nullptr;
   int32_t* d_ps_slot = nullptr;
   int8_t* d_ps_dir = nullptr;
@@ -182,6 +186,7 @@ void fill_args(hlbg_ctx* ctx, StepArgs& a) {
   a.b_ioid = ctx->d_b_ioid;
   a.b_type = ctx->d_b_type;
   a.b_cut = ctx->d_b_cut;
+  a.b_links = ctx->d_b_links;
   a.iolets = ctx->d_iolets;
   a.n_in = (int32_t)ctx->inlets.size();
   a.kernel = ctx->params.kernel;
@@ -230,6 +235,15 @@ int launch_collide(hlbg_ctx* ctx, StepArgs& a, cudaStream_t st) {
     default: launch_stream_collide_2(a, ctx->d_block_xyz, st); break;
   }
   CK(cudaGetLastError());
+  // the all-slots kernel leaves iolet links to k_iolet_links; the list kernel does them itself
+  if (!a.list && ctx->n_io_rec > 0) {
+    switch (ctx->prec) {
+      case 0: launch_iolet_links_0(a, ctx->d_io_rec, ctx->d_rec_slot, ctx->n_io_rec, ctx->d_block_xyz, st); break;
+      case 1: launch_iolet_links_1(a, ctx->d_io_rec, ctx->d_rec_slot, ctx->n_io_rec, ctx->d_block_xyz, st); break;
+      default: launch_iolet_links_2(a, ctx->d_io_rec, ctx->d_rec_slot, ctx->n_io_rec, ctx->d_block_xyz, st); break;
+    }
+    CK(cudaGetLastError());
+  }
   return HLBG_OK;
 }
 
@@ -420,6 +434,35 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
         rcut.push_back(ir >= 0 && g->cut_distance ? g->cut_distance[ir * 18 + k] : -1.0f);
   }
   ctx->nrec = (int64_t)rw.size();
+  // Per-record link codes with StreamerTypeFactory's precedence (iolet delegate for
+  // types 2-5, wall delegate for types 1, 4, 5, else bulk) resolved on the host.
+  std::vector<uint64_t> rlinks((size_t)ctx->nrec, 0);
+  parallel_for(ctx->nrec, [&](int64_t r) {
+    const int64_t s = ctx->h_rec_slot[r];
+    const int ct = rtype[r];
+    const bool can_wall = (ct == 1 || ct == 4 || ct == 5), can_iolet = ct >= 2;
+    uint64_t codes = 0;
+    for (int d = 0; d < 19; ++d) {
+      uint64_t c = HLBG_LC_PUSH;
+      const bool wbit = d > 0 && ((rw[r] >> (d - 1)) & 1u);
+      const bool ibit = d > 0 && ((ri[r] >> (d - 1)) & 1u);
+      if (can_iolet && ibit) {
+        c = HLBG_LC_IOLET;
+      } else if (can_wall && wbit) {
+        c = HLBG_LC_BOUNCE;
+        if (ctx->params.wall == HLBG_WALL_BFL) {
+          const int inv = HINV[d];
+          const float q = rcut[r * 18 + d - 1];
+          if (!(((rw[r] >> (inv - 1)) & 1u) || q < 0.5f)) c = HLBG_LC_BFL;
+        }
+      } else if (d > 0) {
+        int64_t n = neighbour(s, d);
+        if (n < 0 || !fluid(n)) c = HLBG_LC_SKIP;  // the rubbish site
+      }
+      codes |= c << (3 * d);
+    }
+    rlinks[r] = codes;
+  });
   std::vector<uint8_t> bulk((size_t)nb, 0);
   for (int64_t b = 0; b < nb; ++b) {
     bool all = true;
@@ -468,6 +511,19 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   if ((rc = upload(ctx, &ctx->d_b_ioid, rid))) return rc;
   if ((rc = upload(ctx, &ctx->d_b_type, rtype))) return rc;
   if (want_cut && (rc = upload(ctx, &ctx->d_b_cut, rcut))) return rc;
+  if ((rc = upload(ctx, &ctx->d_b_links, rlinks))) return rc;
+  if ((rc = upload(ctx, &ctx->d_rec_slot, ctx->h_rec_slot))) return rc;
+  {
+    std::vector<int32_t> io_rec;
+    for (int64_t r = 0; r < ctx->nrec; ++r)
+      for (int d = 1; d < 19; ++d)
+        if (((rlinks[r] >> (3 * d)) & 7u) == HLBG_LC_IOLET) {
+          io_rec.push_back((int32_t)r);
+          break;
+        }
+    ctx->n_io_rec = (int64_t)io_rec.size();
+    if ((rc = upload(ctx, &ctx->d_io_rec, io_rec))) return rc;
+  }
   if ((rc = upload(ctx, &ctx->d_ref2slot, ctx->h_ref2slot))) return rc;
   if ((rc = upload(ctx, &ctx->d_ps_slot, ctx->h_ps_slot))) return rc;
   if ((rc = upload(ctx, &ctx->d_ps_dir, ctx->h_ps_dir))) return rc;
@@ -502,7 +558,8 @@ void hlbg_destroy(hlbg_ctx* ctx) {
   if (!ctx) return;
   void* ptrs[] = {ctx->f[0],        ctx->f[1],        ctx->d_block_nbr, ctx->d_block_xyz,
                   ctx->d_site_code, ctx->d_block_bulk, ctx->d_b_wall,   ctx->d_b_iolet,
-                  ctx->d_b_ioid,    ctx->d_b_type,    ctx->d_b_cut,     ctx->d_ref2slot,
+                  ctx->d_b_ioid,    ctx->d_b_type,    ctx->d_b_cut,     ctx->d_ref2slot, ctx->d_b_links,
+                  ctx->d_rec_slot,  ctx->d_io_rec,
                   ctx->d_ps_slot,   ctx->d_ps_dir,    ctx->d_ps_q,      ctx->d_iolets,
                   ctx->d_io_tab,    ctx->d_stage,     ctx->d_stage_rho, ctx->d_stage_u,
                   ctx->d_list,      ctx->d_part,      ctx->d_part_bad};
@@ -602,6 +659,10 @@ int hlbg_create(const hlbg_geometry* g, const hlbg_params* p, const hlbg_iolet* 
 
 int64_t hlbg_site_count(const hlbg_ctx* ctx) { return ctx ? ctx->nsites : 0; }
 int64_t hlbg_slot_count(const hlbg_ctx* ctx) { return ctx ? ctx->nslot : 0; }
+int32_t hlbg_launches_per_step(const hlbg_ctx* ctx) {
+  if (!ctx) return 0;
+  return 1 + (ctx->n_io_rec > 0 ? 1 : 0) + (ctx->params.wall == HLBG_WALL_BFL && ctx->n_ps > 0 ? 1 : 0);
+}
 size_t hlbg_device_bytes(const hlbg_ctx* ctx) { return ctx ? ctx->dev_bytes : 0; }
 
 int hlbg_collision_counts(const hlbg_ctx* ctx, int64_t counts[6]) {

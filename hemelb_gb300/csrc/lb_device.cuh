@@ -32,6 +32,13 @@ namespace hlbg {
 constexpr int Q = 19;
 constexpr int kSites = 512;
 
+// Link codes of a boundary record, 3 bits per direction (bits 3d..3d+2).
+#define HLBG_LC_PUSH 0ull  // stream to the neighbour (BulkLink)
+#define HLBG_LC_SKIP 1ull       // neighbour not fluid: the reference writes the rubbish site
+#define HLBG_LC_BOUNCE 2ull     // SimpleBounceBack, or BFL falling back to it
+#define HLBG_LC_BFL 3ull        // BFL eq. 5b interpolation
+#define HLBG_LC_IOLET 4ull      // Nash or Ladd iolet link
+
 static __constant__ int c_cx[Q] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
 static __constant__ int c_cy[Q] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
 static __constant__ int c_cz[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
@@ -81,6 +88,7 @@ struct StepArgs {
   const int32_t* b_ioid;
   const int8_t* b_type;
   const float* b_cut;  // [nrec * 18] or null
+  const uint64_t* b_links;  // [nrec] 3-bit link code per direction (HLBG_LC_*)
   const int32_t* list;  // optional slot list (per-range drop-in), null = all slots
   int64_t list_count;
   const IoletDev* iolets;     // [n_in + n_out]
@@ -227,32 +235,30 @@ __device__ __forceinline__ float geq_dev(float dr, float inv_rho, float m2x15, f
   return weight_f(i) * ((dr - m2x15 * inv_rho) + mde * (3.f + 4.5f * inv_rho * mde));
 }
 
+// Collide on opposite-direction pairs (i, i+1): with e = f_eq - w split into its
+// even part w (A + 4.5 (c.m)^2 / rho) and odd part 3 w (c.m), the symmetric and
+// antisymmetric non-equilibrium parts relax with omega+ and omega- (TRT,
+// Code/lb/kernels/TRT.h:160-188); LBGK is the case omega- = omega+.
 __device__ __forceinline__ void collide_dev(const StepArgs& a, const float* g, float& dr, float& mx,
                                             float& my, float& mz, float* gpost) {
   moments_dev(g, dr, mx, my, mz);
   const float inv_rho = 1.f / (1.f + dr);
-  const float m2x15 = 1.5f * (mx * mx + my * my + mz * mz);
-  if (a.kernel == 0) {
+  const float A = dr - 1.5f * (mx * mx + my * my + mz * mz) * inv_rho;
+  const float c45 = 4.5f * inv_rho;
+  const float wp = a.omega_f;
+  const float wm = a.kernel == 0 ? a.omega_f : a.omega_minus_f;
+  gpost[0] = g[0] + wp * (g[0] - weight_f(0) * A);
 #pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      const float ge = geq_dev(dr, inv_rho, m2x15, mx, my, mz, i);
-      gpost[i] = g[i] + a.omega_f * (g[i] - ge);
-    }
-  } else {
-    {
-      const float ge = geq_dev(dr, inv_rho, m2x15, mx, my, mz, 0);
-      gpost[0] = g[0] + a.omega_f * (g[0] - ge);
-    }
-#pragma unroll
-    for (int i = 1; i < Q; i += 2) {
-      const int ib = i + 1;
-      const float ni = g[i] - geq_dev(dr, inv_rho, m2x15, mx, my, mz, i);
-      const float nb = g[ib] - geq_dev(dr, inv_rho, m2x15, mx, my, mz, ib);
-      const float sym = 0.5f * a.omega_f * (ni + nb);
-      const float asym = 0.5f * a.omega_minus_f * (ni - nb);
-      gpost[i] = g[i] + sym + asym;
-      gpost[ib] = g[ib] + sym - asym;
-    }
+  for (int i = 1; i < Q; i += 2) {
+    const float mde = Lat::cx(i) * mx + Lat::cy(i) * my + Lat::cz(i) * mz;
+    const float w = weight_f(i);
+    const float e_sym = w * fmaf(c45 * mde, mde, A);
+    const float e_asym = (3.f * w) * mde;
+    const float sym = fmaf(0.5f, g[i] + g[i + 1], -e_sym);
+    const float asym = fmaf(0.5f, g[i] - g[i + 1], -e_asym);
+    const float t = wp * sym, u = wm * asym;
+    gpost[i] = g[i] + t + u;
+    gpost[i + 1] = g[i + 1] + t - u;
   }
 }
 

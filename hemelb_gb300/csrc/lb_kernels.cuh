@@ -123,6 +123,12 @@ struct SmemBase {
   const int64_t* sh;
   __device__ __forceinline__ int64_t operator()(int k) const { return sh[k]; }
 };
+struct ShflBase {
+  int32_t reg;  // lane k < 27 holds neighbour block k
+  __device__ __forceinline__ int64_t operator()(int k) const {
+    return (int64_t)__shfl_sync(0xffffffffu, reg, k) * (Q * kSites);
+  }
+};
 struct GlobalBase {
   const int32_t* tab;
   __device__ __forceinline__ int64_t operator()(int k) const {
@@ -150,6 +156,76 @@ template <int P>
 struct PushAll<P, Q> {
   template <class S, class T, class B>
   static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int, int, int, const T*) {}
+};
+
+// Pushes of the all-slots kernel: every lane takes part in the shuffles, only
+// bulk sites store.
+template <int P, int D>
+struct PushBulk {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, int x, int y,
+                                             int z, bool store, const T* fpost) {
+    constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
+    const int xx = x + cx, yy = y + cy, zz = z + cz;
+    const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
+    const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+    const int64_t nb = base(k);
+    if (store) Store<P>::store(fn + nb, D * kSites + tl, fpost[D], a);
+    PushBulk<P, D + 1>::run(fn, a, base, x, y, z, store, fpost);
+  }
+};
+template <int P>
+struct PushBulk<P, Q> {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int, int, int, bool,
+                                             const T*) {}
+};
+
+// Pushes of a warp that holds at least one boundary site.  Every lane computes
+// the bulk target (shuffles stay converged); a boundary lane then redirects the
+// link by its precomputed code: skip (the reference's rubbish site), bounce-back
+// into its own inverse slot, BFL eq. 5b, or an iolet value.
+template <int P, int D>
+struct PushMixed {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, int x, int y,
+                                             int z, int l, int64_t own, bool active, uint64_t links,
+                                             int64_t r, int type, int ioid, const T* fpost, T m0,
+                                             T mx, T my, T mz, int64_t b,
+                                             const int32_t* __restrict__ block_xyz) {
+    constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
+    constexpr int inv = Lat::inv(D);
+    const int xx = x + cx, yy = y + cy, zz = z + cz;
+    const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
+    const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+    const int64_t nb = base(k);
+    const unsigned lc = (unsigned)((links >> (3 * D)) & 7u);
+    int64_t off = nb + D * kSites + tl;
+    T v = fpost[D];
+    bool st = active;
+    if (lc != HLBG_LC_PUSH) {
+      if (lc == HLBG_LC_SKIP) {
+        st = false;
+      } else {
+        off = own + inv * kSites + l;
+        if (lc == HLBG_LC_BFL) {
+          const T q = (T)a.b_cut[r * (Q - 1) + D - 1];
+          v = (fpost[D] + ((T)2.0 * q - (T)1) * fpost[inv]) / ((T)2.0 * q);
+        }
+        if (lc == HLBG_LC_IOLET) st = false;  // written by k_iolet_links
+      }
+    }
+    if (st) Store<P>::store(fn, off, v, a);
+    PushMixed<P, D + 1>::run(fn, a, base, x, y, z, l, own, active, links, r, type, ioid, fpost, m0,
+                             mx, my, mz, b, block_xyz);
+  }
+};
+template <int P>
+struct PushMixed<P, Q> {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int, int, int, int,
+                                             int64_t, bool, uint64_t, int64_t, int, int, const T*,
+                                             T, T, T, T, int64_t, const int32_t*) {}
 };
 
 // ---------------------------------------------------------------------------
@@ -183,23 +259,50 @@ __device__ __forceinline__ void site_update(const StepArgs& a, const B& base,
                          (int)a.b_type[r], a.b_ioid[r], r, fpost, m0, mx, my, mz, block_xyz);
 }
 
+// All slots, one thread each.  A warp covers 32 slots of one block; lanes 0..26
+// hold the block's neighbour table and serve it to the bulk pushes by shuffle, so
+// every lane of a warp with any fluid site stays converged through the pushes.
 template <int P>
 __global__ void __launch_bounds__(HLBG_SC_THREADS, (P == 0 ? HLBG_SC_MINB64 : HLBG_SC_MINB))
     k_stream_collide(StepArgs a, const int32_t* block_xyz) {
-  __shared__ int64_t sh_base[27];
-  const int64_t s0 = (int64_t)blockIdx.x * HLBG_SC_THREADS;
-  const int64_t b = s0 >> 9;
+  using St = Store<P>;
+  using S = typename St::S;
+  using T = typename Calc<P>::T;
+  const int64_t s = (int64_t)blockIdx.x * HLBG_SC_THREADS + threadIdx.x;  // < nslot (512 | nslot)
+  const int64_t b = s >> 9;
+  const int lane = threadIdx.x & 31;
   const int32_t* tab = a.block_nbr + b * 27;
-  if (threadIdx.x < 27) {
-    const int32_t nb = tab[threadIdx.x];
-    sh_base[threadIdx.x] = nb < 0 ? (int64_t)-1 : (int64_t)nb * (Q * kSites);
-  }
-  __syncthreads();
-  const int64_t s = s0 + threadIdx.x;
-  if (s >= a.nslot) return;
+  const int32_t tabreg = lane < 27 ? __ldg(tab + lane) : 0;
   const uint32_t code = a.block_bulk[b] ? 1u : a.site_code[s];
-  if (code == 0) return;
-  site_update<P>(a, SmemBase{sh_base}, tab, s, code, block_xyz);
+  if (__ballot_sync(0xffffffffu, code != 0) == 0) return;
+  const int l = (int)(s & (kSites - 1));
+  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + l;
+  S* fn = static_cast<S*>(a.f_new);
+  T f[Q], fpost[Q];
+  if (code != 0) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
+  } else {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = (T)(P == 0 ? weight_d(i) : 0.0);
+  }
+  T m0, mx, my, mz;
+  if constexpr (P == 0)
+    collide64(a, f, m0, mx, my, mz, fpost);
+  else
+    collide_dev(a, f, m0, mx, my, mz, fpost);
+  const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
+  const bool bnd = code >= 2;
+  if (__ballot_sync(0xffffffffu, bnd) == 0) {
+    PushBulk<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, code == 1, fpost);
+  } else {
+    const int64_t r = bnd ? (int64_t)code - 2 : 0;
+    const uint64_t links = bnd ? a.b_links[r] : 0ull;
+    const int type = bnd ? (int)a.b_type[r] : 0;
+    const int ioid = bnd ? a.b_ioid[r] : 0;
+    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, l, b * (Q * kSites), code != 0, links, r,
+                         type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
+  }
 }
 
 template <int P>
@@ -212,6 +315,53 @@ __global__ void __launch_bounds__(256) k_stream_collide_list(StepArgs a, const i
   if (code == 0) return;
   const int32_t* tab = a.block_nbr + b * 27;
   site_update<P>(a, GlobalBase{tab}, tab, s, code, block_xyz);
+}
+
+// Iolet links (Nash / Ladd) of the sites listed in `rec`: the site's collision is
+// recomputed from f_old with the same arithmetic as k_stream_collide, and each iolet
+// link writes the site's own inverse-direction slot.  These slots have no other
+// writer, so this launch and k_stream_collide may run in either order.
+template <int P>
+__global__ void __launch_bounds__(128) k_iolet_links(StepArgs a, const int32_t* __restrict__ rec,
+                                                     const int32_t* __restrict__ rec_slot, int64_t n,
+                                                     const int32_t* __restrict__ block_xyz) {
+  using St = Store<P>;
+  using S = typename St::S;
+  using T = typename Calc<P>::T;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t r = rec[i];
+  const int64_t s = rec_slot[r];
+  const int64_t b = s >> 9;
+  const int l = (int)(s & (kSites - 1));
+  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + l;
+  S* fn = static_cast<S*>(a.f_new) + b * (Q * kSites) + l;
+  T f[Q], fpost[Q];
+#pragma unroll
+  for (int d = 0; d < Q; ++d) f[d] = St::load(fo, d * kSites, a);
+  T m0, mx, my, mz;
+  if constexpr (P == 0)
+    collide64(a, f, m0, mx, my, mz, fpost);
+  else
+    collide_dev(a, f, m0, mx, my, mz, fpost);
+  const uint64_t links = a.b_links[r];
+  const int type = a.b_type[r];
+  const int ioid = a.b_ioid[r];
+  const bool is_inlet = (type == 2 || type == 4);
+  const int gi = is_inlet ? ioid : a.n_in + ioid;
+  const int model = is_inlet ? a.inlet_model : a.outlet_model;
+  const int gx = block_xyz[3 * b] * 8 + (l >> 6), gy = block_xyz[3 * b + 1] * 8 + ((l >> 3) & 7),
+            gz = block_xyz[3 * b + 2] * 8 + (l & 7);
+#pragma unroll 1
+  for (int d = 1; d < Q; ++d) {
+    if (((links >> (3 * d)) & 7u) != HLBG_LC_IOLET) continue;
+    T fp = fpost[0];
+#pragma unroll
+    for (int e = 1; e < Q; ++e)
+      if (e == d) fp = fpost[e];
+    const T v = iolet_link_value<P>(a, gi, model, d, fp, m0, mx, my, mz, gx, gy, gz);
+    St::store(fn, c_inv[d] * kSites, v, a);
+  }
 }
 
 // BouzidiFirdaousLallemandLink::PostStepLink (BouzidiFirdaousLallemand.h:336-357)
@@ -518,6 +668,11 @@ static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, in
       unsigned g = (unsigned)((a.nslot + HLBG_SC_THREADS - 1) / HLBG_SC_THREADS);               \
       if (g) k_stream_collide<P><<<g, HLBG_SC_THREADS, 0, st>>>(a, bxyz);                       \
     }                                                                                           \
+  }                                                                                             \
+  void launch_iolet_links_##P(const StepArgs& a, const int32_t* rec, const int32_t* rec_slot,    \
+                              int64_t n, const int32_t* bxyz, cudaStream_t st) {                \
+    unsigned g = (unsigned)((n + 127) / 128);                                                   \
+    if (g) k_iolet_links<P><<<g, 128, 0, st>>>(a, rec, rec_slot, n, bxyz);                      \
   }                                                                                             \
   void launch_post_step_##P(const PostArgs& p, cudaStream_t st) {                               \
     unsigned g = (unsigned)((p.count + 255) / 256);                                             \

@@ -67,6 +67,8 @@ struct MonitorArgs {
 
 #define HLBG_DECLARE(P)                                                              \
   void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st); \
+  void launch_iolet_links_##P(const StepArgs& a, const int32_t* rec, const int32_t* rec_slot, \
+                              int64_t n, const int32_t* bxyz, cudaStream_t st);          \
   void launch_post_step_##P(const PostArgs& p, cudaStream_t st);                     \
   void launch_init_uniform_##P(const InitArgs& ia, cudaStream_t st);                 \
   void launch_init_field_##P(const FieldArgs& fa, cudaStream_t st);                  \

@@ -73,12 +73,6 @@ extern "C" {
 #define HLBG_SITE_INLET 2
 #define HLBG_SITE_OUTLET 3
 
-/* link types of the synthetic generator (io/formats/geometry CutType) */
-#define HLBG_LINK_NONE 0
-#define HLBG_LINK_WALL 1
-#define HLBG_LINK_INLET 2
-#define HLBG_LINK_OUTLET 3
-
 /*
  * Sparse block geometry: the content of a GmyReadResult
  * (Code/geometry/GmyReadResult.h) restricted to what the LB update reads.
@@ -172,6 +166,8 @@ const char *hlbg_last_error(const hlbg_ctx *ctx);
 
 int64_t hlbg_site_count(const hlbg_ctx *ctx);   /* fluid sites N */
 int64_t hlbg_slot_count(const hlbg_ctx *ctx);   /* device slots (n_blocks * 512) */
+/* Kernel launches one hlbg_step time step makes (stream-collide, iolet links, BFL PostStep). */
+int32_t hlbg_launches_per_step(const hlbg_ctx *ctx);
 int hlbg_collision_counts(const hlbg_ctx *ctx, int64_t counts[6]);
 size_t hlbg_device_bytes(const hlbg_ctx *ctx);
 
