@@ -20,6 +20,8 @@ FP64, FP32DEV, FP16 = 0, 1, 2
 IOLET_COSINE, IOLET_PARABOLIC, IOLET_PULSATILE = 0, 1, 2
 SITE_FLUID, SITE_INLET, SITE_OUTLET = 1, 2, 3
 
+NOALLOC_MAX_SLOTS = 65536 * 256
+
 ERRORS = {1: "INVAL", 2: "OOM", 3: "CUDA", 4: "UNSTABLE", 5: "TIMEOUT", 6: "STATE"}
 
 
@@ -96,6 +98,7 @@ SIGNATURES = {
     "hlbg_put_f_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "hlbg_get_macro": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "hlbg_reduce": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "hlbg_reduce_noalloc": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "hlbg_iolet_density": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64,
                                      C.POINTER(C.c_double)]),
     "hlbg_time_steps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),

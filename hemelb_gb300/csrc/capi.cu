@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
@@ -976,6 +977,86 @@ int hlbg_reduce(hlbg_ctx* ctx, hlbg_stats* out) {
                        ctx->stream));
   CK(cudaMemcpyAsync(&bad, ctx->d_part_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                      ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  out->mass = res[0];
+  out->max_du = res[1];
+  out->min_f = res[2];
+  out->unstable_sites = (int64_t)bad;
+  out->time_step = (int64_t)ctx->t1;
+  return bad ? HLBG_ERR_UNSTABLE : HLBG_OK;
+}
+
+}  // extern "C"
+
+// ---- allocation-free StabilityTester reduction --------------------------------
+// Scratch of hlbg_reduce_noalloc: the per-CTA partials of k_monitor (mass, max|du|,
+// min f, unstable count) for at most kNoAllocParts reduction blocks, laid out as
+// four consecutive runs of kNoAllocParts values.  Every GPU that loads the library
+// holds these 2 MiB until the process exits.  Host code must not use the symbol
+// as a pointer: the device address comes from cudaGetSymbolAddress, once per device.
+static constexpr int64_t kNoAllocParts = HLBG_NOALLOC_MAX_SLOTS / 256;
+static __device__ __align__(256) double g_reduce_scratch[4 * kNoAllocParts];
+
+namespace {
+std::mutex g_scratch_mu;
+void* g_scratch_addr[256] = {};
+
+int scratch_address(hlbg_ctx* ctx, double** out) {
+  int dev = -1;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail(ctx, HLBG_ERR_CUDA, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(ctx, HLBG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_scratch_addr[dev] = p;
+  }
+  *out = static_cast<double*>(g_scratch_addr[dev]);
+  return HLBG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int hlbg_reduce_noalloc(hlbg_ctx* ctx, hlbg_stats* out) {
+  if (!ctx || !out) return HLBG_ERR_INVAL;
+  const int64_t nparts = (ctx->nslot + 255) / 256;
+  if (nparts > kNoAllocParts)
+    return fail(ctx, HLBG_ERR_INVAL,
+                "hlbg_reduce_noalloc: " + std::to_string(ctx->nslot) + " slots exceed its limit of " +
+                    std::to_string(HLBG_NOALLOC_MAX_SLOTS) + " (use hlbg_reduce)");
+  double* scratch = nullptr;
+  int rc = scratch_address(ctx, &scratch);
+  if (rc) return rc;
+  // Every partial k_monitor reads is written earlier in the same call (one per
+  // CTA, then the final pass into element 0 of each run), so nothing needs clearing.
+  MonitorArgs ma{};
+  ma.f_cur = ctx->f[ctx->cur];
+  ma.f_prev = ctx->f[ctx->cur ^ 1];
+  ma.stride = ctx->nslot;
+  ma.nslot = ctx->nslot;
+  ma.site_code = ctx->d_site_code;
+  ma.block_bulk = ctx->d_block_bulk;
+  ma.part_mass = scratch;
+  ma.part_max = scratch + kNoAllocParts;
+  ma.part_min = scratch + 2 * kNoAllocParts;
+  ma.part_bad = reinterpret_cast<unsigned long long*>(scratch + 3 * kNoAllocParts);
+  ma.fp16_scale = ctx->fp16_scale;
+  ma.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+  switch (ctx->prec) {
+    case 0: launch_monitor_0(ma, 0, ctx->stream); break;
+    case 1: launch_monitor_1(ma, 0, ctx->stream); break;
+    default: launch_monitor_2(ma, 0, ctx->stream); break;
+  }
+  CK(cudaGetLastError());
+  double res[3];
+  unsigned long long bad = 0;
+  CK(cudaMemcpyAsync(&res[0], ma.part_mass, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&res[1], ma.part_max, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&res[2], ma.part_min, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&bad, ma.part_bad, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   out->mass = res[0];
   out->max_du = res[1];

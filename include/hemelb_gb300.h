@@ -209,6 +209,21 @@ int hlbg_get_macro(hlbg_ctx *ctx, double *rho, double *u);
  * velocity, min f, unstable count).  Synchronous. */
 int hlbg_reduce(hlbg_ctx *ctx, hlbg_stats *out);
 
+/* Allocation-free variant of hlbg_reduce.  No counterpart in the reference: it
+ * exists for callers that must not allocate device memory once their time loop
+ * runs -- a host framework that reserves its whole device-memory budget up front,
+ * or one for which a cudaMalloc in the loop would synchronise the device and stall
+ * overlapped work -- whereas hlbg_reduce allocates its partial-sum buffer on its
+ * first call.  Scratch is a fixed 2 MiB static device array (one partial per
+ * 256-slot reduction block), so geometries are limited to HLBG_NOALLOC_MAX_SLOTS
+ * slots (hlbg_slot_count); larger ones are rejected with HLBG_ERR_INVAL.  The
+ * first call on a device (with that device current) looks up the array's device
+ * address; make that first call before any stream capture.  All calls on a
+ * device share the array: calls that overlap on the GPU race.  Synchronous, same
+ * results as hlbg_reduce. */
+#define HLBG_NOALLOC_MAX_SLOTS (65536LL * 256LL)
+int hlbg_reduce_noalloc(hlbg_ctx *ctx, hlbg_stats *out);
+
 /* Per-step iolet values the host computed for the steps [t, t+n) (for tests). */
 int hlbg_iolet_density(const hlbg_ctx *ctx, int32_t is_outlet, int32_t index, uint64_t t,
                        double *density);
