@@ -62,6 +62,9 @@ def parse():
                     help="fluid sites in the CPU sample (Morton-contiguous blocks)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--members", type=int, default=512)
+    ap.add_argument("--report", default=None, choices=["precision", "steady", "ensemble"],
+                    help="print a report instead of the throughput line")
     return ap.parse_args()
 
 
@@ -257,6 +260,18 @@ def run_reference_arm(args):
 
 def main():
     args = parse()
+    if args.report:
+        from hemelb_gb300 import cases, reports
+        if args.report == "precision":
+            print(json.dumps(reports.precision_report(steps=args.steps)), flush=True)
+        elif args.report == "ensemble":
+            print(json.dumps(reports.ensemble_report(args.members, steps=args.steps,
+                                                     warmup=args.warmup)), flush=True)
+        else:
+            c = cases.pipe()
+            # Poiseuille centre-line speed of the pipe's pressure drop, as U_ref
+            print(json.dumps(reports.steady_report(c, u_ref=0.01)), flush=True)
+        return
     if args.impl == "reference":
         if RANK == 0:
             run_reference_arm(args)

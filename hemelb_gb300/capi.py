@@ -69,6 +69,10 @@ SIGNATURES = {
                                       C.POINTER(C.c_void_p)]),
     "hlbg_synth_tree": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                   C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "hlbg_synth_ensemble": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "hlbg_synth_members": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.POINTER(C.c_int32)),
+                                     C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.POINTER(C.c_double)),
+                                     C.POINTER(C.POINTER(C.c_int64))]),
     "hlbg_synth_view": (C.c_int, [C.c_void_p, C.POINTER(Geometry), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "hlbg_synth_iolet": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double * 3, C.c_double * 3,
@@ -88,6 +92,9 @@ SIGNATURES = {
     "hlbg_init_equilibrium_field": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "hlbg_step": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "hlbg_sync": (C.c_int, [C.c_void_p]),
+    "hlbg_step_graph": (C.c_int, [C.c_void_p, C.c_int32]),
+    "hlbg_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "hlbg_set_block_tau": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_stream_and_collide_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "hlbg_post_step_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "hlbg_swap": (C.c_int, [C.c_void_p]),

@@ -84,3 +84,55 @@ def stenosis(radius: float = 10.0, length: int = 80, depth: float = 0.5, tau: fl
     p = LbmParameters(tau=tau, kernel=capi.KERNEL_LBGK, wall=capi.WALL_SBB,
                       inlet=capi.IOLET_LADD, outlet=capi.IOLET_NASH, precision=precision)
     return Case("stenosis_r%g_l%d_d%.2f" % (radius, length, depth), g, p, inl, outl, 0)
+
+
+def ensemble(n_members: int = 512, seed: int = 2024, precision=capi.FP32DEV, peak: float = 0.02,
+             period: float = 1000.0):
+    """Batched ensemble of seeded stenosed pipes in one geometry (one cell per
+    member), per-member tau, pulsatile Ladd inlets and Nash outlets.  Returns the
+    Case (its solver() sets the per-block tau) and the member table."""
+    g = SyntheticGeometry.ensemble(seed, n_members, 19)
+    block_member, tau, shape, sites = g.members()
+    inl, outl = [], []
+    for k in range(g.n_inlets):
+        pos, nrm, r = g.iolet(False, k)
+        inl.append(InOutLetParabolicVelocity(pos, nrm, radius=r, max_speed=peak, pulsatile_period=period))
+    for k in range(g.n_outlets):
+        pos, nrm, _ = g.iolet(True, k)
+        outl.append(InOutLetCosine(pos, nrm, density_mean=1.0))
+    p = LbmParameters(tau=0.8, kernel=capi.KERNEL_LBGK, wall=capi.WALL_SBB,
+                      inlet=capi.IOLET_LADD, outlet=capi.IOLET_NASH, precision=precision)
+    case = EnsembleCase("ensemble_%d_s%d" % (n_members, seed), g, p, inl, outl, 0)
+    case.block_tau = tau[block_member]
+    case.members = {"tau": tau, "shape": shape, "sites": sites, "block_member": block_member,
+                    "peak": peak, "period": period}
+    return case
+
+
+class EnsembleCase(Case):
+    """A Case whose solver carries one relaxation time per member."""
+
+    block_tau = None
+    members = None
+
+    def solver(self, precision=None):
+        s = super().solver(precision)
+        s.SetBlockTau(self.block_tau)
+        return s
+
+    def member_case(self, m: int, precision=capi.FP32DEV) -> Case:
+        """Member m as a standalone geometry (same voxels up to a translation)."""
+        R, L, depth = self.members["shape"][m]
+        g = SyntheticGeometry.stenosis(R, int(L), depth, 19, with_cuts=True)
+        inl, outl = [], []
+        for k in range(g.n_inlets):
+            pos, nrm, r = g.iolet(False, k)
+            inl.append(InOutLetParabolicVelocity(pos, nrm, radius=r, max_speed=self.members["peak"],
+                                                 pulsatile_period=self.members["period"]))
+        for k in range(g.n_outlets):
+            pos, nrm, _ = g.iolet(True, k)
+            outl.append(InOutLetCosine(pos, nrm, density_mean=1.0))
+        p = LbmParameters(tau=float(self.members["tau"][m]), kernel=capi.KERNEL_LBGK,
+                          wall=capi.WALL_SBB, inlet=capi.IOLET_LADD, outlet=capi.IOLET_NASH,
+                          precision=precision)
+        return Case("member_%d" % m, g, p, inl, outl, 0)

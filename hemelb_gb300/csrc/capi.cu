@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <map>
 #include <new>
 #include <string>
 #include <thread>
@@ -107,6 +108,14 @@ struct hlbg_ctx {
   float* d_b_cut = nullptr;
   uint64_t* d_b_links = nullptr;  // 3-bit link code per direction (see lb_device.cuh)
   int32_t* d_rec_slot = nullptr;  // slot of each record
+  std::vector<int32_t> h_new_of_old;  // device block index of each input block
+  double* d_blk_omega = nullptr;      // optional per-block (omega+, omega-)
+  // CUDA graphs of k steps, keyed by (k, parity of the current array)
+  struct GraphKey {
+    int n, cur;
+    bool operator<(const GraphKey& o) const { return n != o.n ? n < o.n : cur < o.cur; }
+  };
+  std::map<GraphKey, cudaGraphExec_t> graphs;
   int32_t* d_io_rec = nullptr;    // records with at least one iolet link
   int64_t n_io_rec = 0;
   int32_t* d_ref2slot = nullptr;
@@ -135,6 +144,7 @@ struct hlbg_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t dev_bytes = 0;
   float fp16_scale = 1024.f;
+  int sc_variant = 0;  // chosen by hlbg_autotune
   bool initialised = false;
 };
 
@@ -188,6 +198,7 @@ void fill_args(hlbg_ctx* ctx, StepArgs& a) {
   a.b_type = ctx->d_b_type;
   a.b_cut = ctx->d_b_cut;
   a.b_links = ctx->d_b_links;
+  a.blk_omega = ctx->d_blk_omega;
   a.iolets = ctx->d_iolets;
   a.n_in = (int32_t)ctx->inlets.size();
   a.kernel = ctx->params.kernel;
@@ -231,9 +242,9 @@ double iolet_umax(const hlbg_iolet& io, uint64_t t) {
 
 int launch_collide(hlbg_ctx* ctx, StepArgs& a, cudaStream_t st) {
   switch (ctx->prec) {
-    case 0: launch_stream_collide_0(a, ctx->d_block_xyz, st); break;
-    case 1: launch_stream_collide_1(a, ctx->d_block_xyz, st); break;
-    default: launch_stream_collide_2(a, ctx->d_block_xyz, st); break;
+    case 0: launch_stream_collide_0(a, ctx->d_block_xyz, st, ctx->sc_variant); break;
+    case 1: launch_stream_collide_1(a, ctx->d_block_xyz, st, ctx->sc_variant); break;
+    default: launch_stream_collide_2(a, ctx->d_block_xyz, st, ctx->sc_variant); break;
   }
   CK(cudaGetLastError());
   // the all-slots kernel leaves iolet links to k_iolet_links; the list kernel does them itself
@@ -316,15 +327,21 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     return fail(ctx, HLBG_ERR_INVAL, "geometry has no blocks");
   if ((int64_t)NX * NY * NZ > (1ll << 31)) return fail(ctx, HLBG_ERR_INVAL, "block grid too large");
   if (nb * 512 >= (1ll << 31)) return fail(ctx, HLBG_ERR_INVAL, "more than 2^31 slots");
-  // blocks in Morton order
+  // Device block order: z-columns (2-D Morton order of (x, y), then z).  The two
+  // writers of every z-shifted row of a push are z-adjacent blocks; running them
+  // back to back lets their partial 32-byte sectors merge in L2.  The reference's
+  // own numbering (3-D Morton order) is kept separately in ref_rank below.
   std::vector<std::pair<uint64_t, int64_t>> order((size_t)nb);
+  std::vector<std::pair<uint64_t, int64_t>> ref_order((size_t)nb);
   for (int64_t b = 0; b < nb; ++b) {
     int32_t x = g->block_coords[3 * b], y = g->block_coords[3 * b + 1], z = g->block_coords[3 * b + 2];
     if (x < 0 || y < 0 || z < 0 || x >= NX || y >= NY || z >= NZ)
       return fail(ctx, HLBG_ERR_INVAL, "block coordinate outside the block grid");
-    order[b] = {morton3(x, y, z), b};
+    order[b] = {(morton3(x, y, 0) << 16) | (uint64_t)z, b};
+    ref_order[b] = {morton3(x, y, z), b};
   }
   std::sort(order.begin(), order.end());
+  std::sort(ref_order.begin(), ref_order.end());
   std::vector<int32_t> new_of_old((size_t)nb);
   std::vector<int32_t> grid((size_t)NX * NY * NZ, -1);
   ctx->h_block_xyz.resize((size_t)nb * 3);
@@ -341,6 +358,7 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     ctx->h_block_xyz[3 * nbi + 2] = z;
     for (int w = 0; w < 8; ++w) mask[nbi * 8 + w] = g->fluid_mask[ob * 8 + w];
   }
+  ctx->h_new_of_old = new_of_old;
   std::vector<int32_t> bnbr((size_t)nb * 27);
   parallel_for(nb, [&](int64_t b) {
     int32_t x = ctx->h_block_xyz[3 * b], y = ctx->h_block_xyz[3 * b + 1], z = ctx->h_block_xyz[3 * b + 2];
@@ -480,8 +498,13 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   ctx->nsites = off[5] + cnt[5];
   for (int t = 0; t < 6; ++t) ctx->type_count[t] = cnt[t];
   ctx->h_ref2slot.assign((size_t)ctx->nsites, 0);
-  for (int64_t s = 0; s < nslot; ++s)
-    if (site_ctype[s] >= 0) ctx->h_ref2slot[off[site_ctype[s]]++] = (int32_t)s;
+  for (int64_t rb = 0; rb < nb; ++rb) {
+    const int64_t b = new_of_old[ref_order[rb].second];
+    for (int l = 0; l < 512; ++l) {
+      const int64_t s = b * 512 + l;
+      if (site_ctype[s] >= 0) ctx->h_ref2slot[off[site_ctype[s]]++] = (int32_t)s;
+    }
+  }
   // BFL PostStep links
   if (want_cut) {
     for (int64_t r = 0; r < ctx->nrec; ++r) {
@@ -566,6 +589,8 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_list,      ctx->d_part,      ctx->d_part_bad};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+  if (ctx->d_blk_omega) cudaFree(ctx->d_blk_omega);
   if (ctx->h_io_tab) cudaFreeHost(ctx->h_io_tab);
   if (ctx->io_copied) cudaEventDestroy(ctx->io_copied);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -770,6 +795,119 @@ int hlbg_step(hlbg_ctx* ctx, int32_t nsteps, void* cuda_stream) {
     }
     done += n;
   }
+  return HLBG_OK;
+}
+
+int hlbg_set_block_tau(hlbg_ctx* ctx, const double* tau) {
+  if (!ctx || !tau) return HLBG_ERR_INVAL;
+  std::vector<double> w((size_t)ctx->nb * 2);
+  for (int64_t ob = 0; ob < ctx->nb; ++ob) {
+    const double t = tau[ob];
+    if (!(t > 0.5)) return fail(ctx, HLBG_ERR_INVAL, "every tau must exceed 0.5");
+    const int64_t b = ctx->h_new_of_old[ob];
+    // LbmParameters::CalcDerivedParams and TRT's second rate, per block
+    w[2 * b] = -1.0 / t;
+    w[2 * b + 1] = -1.0 / (0.5 + (3.0 / 16.0) / (t - 0.5));
+  }
+  if (!ctx->d_blk_omega) {
+    int rc = dev_alloc(ctx, &ctx->d_blk_omega, w.size());
+    if (rc) return rc;
+  }
+  CK(cudaMemcpy(ctx->d_blk_omega, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);  // captured args changed
+  ctx->graphs.clear();
+  return HLBG_OK;
+}
+
+int hlbg_step_graph(hlbg_ctx* ctx, int32_t nsteps) {
+  // nsteps time steps as one CUDA graph launch: the iolet-table copy and every
+  // kernel of every step, captured once per (step count, array parity) and
+  // replayed.  The host refreshes the pinned iolet table before each replay.
+  if (!ctx || nsteps < 0) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  for (int done = 0; done < nsteps;) {
+    const int n = std::min(kStepBatch, nsteps - done);
+    if (ctx->n_io) {
+      CK(cudaEventSynchronize(ctx->io_copied));
+      for (int k = 0; k < n; ++k) {
+        uint64_t t1 = ctx->t1 + k;
+        double* row = ctx->h_io_tab + (size_t)k * 2 * ctx->n_io;
+        int j = 0;
+        for (auto* v : {&ctx->inlets, &ctx->outlets})
+          for (auto& io : *v) {
+            row[j] = iolet_density(ctx, io, t1 - 1);
+            row[ctx->n_io + j] = iolet_umax(io, (uint64_t)(unsigned int)t1);
+            ++j;
+          }
+      }
+    }
+    hlbg_ctx::GraphKey key{n, ctx->cur};
+    auto it = ctx->graphs.find(key);
+    if (it == ctx->graphs.end()) {
+      cudaGraph_t graph = nullptr;
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      int rc = HLBG_OK;
+      if (ctx->n_io) {
+        cudaError_t e = cudaMemcpyAsync(ctx->d_io_tab, ctx->h_io_tab, sizeof(double) * 2 * ctx->n_io * n,
+                                        cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) rc = fail(ctx, HLBG_ERR_CUDA, cudaGetErrorString(e));
+      }
+      const int cur0 = ctx->cur;
+      StepArgs a;
+      for (int k = 0; k < n && !rc; ++k) {
+        fill_args(ctx, a);
+        a.iolet_rho = ctx->d_io_tab + (size_t)k * 2 * ctx->n_io;
+        a.iolet_umax = a.iolet_rho + ctx->n_io;
+        rc = launch_collide(ctx, a, ctx->stream);
+        if (!rc) rc = run_post(ctx, ctx->stream, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps);
+        ctx->cur ^= 1;
+      }
+      ctx->cur = cur0;
+      cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+      if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+      cudaGraphExec_t exec = nullptr;
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+      it = ctx->graphs.emplace(key, exec).first;
+    }
+    CK(cudaGraphLaunch(it->second, ctx->stream));
+    if (ctx->n_io) CK(cudaEventRecord(ctx->io_copied, ctx->stream));
+    ctx->cur ^= (n & 1);
+    ctx->t1 += n;
+    done += n;
+  }
+  return HLBG_OK;
+}
+
+int hlbg_autotune(hlbg_ctx* ctx, int32_t steps_per_trial, int32_t* chosen, float* best_ms) {
+  // Time every launch variant of the stream-and-collide kernel on this context for
+  // steps_per_trial steps (after one untimed step each) and keep the fastest.
+  // Stepping advances the state, exactly as hlbg_step would.
+  if (!ctx || steps_per_trial < 1) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  int best = ctx->sc_variant;
+  float best_t = 1e30f;
+  for (int v = 0; v < (ctx->prec == 0 ? 1 : kSCVariants); ++v) {
+    ctx->sc_variant = v;
+    int rc = hlbg_step(ctx, 1, nullptr);
+    if (rc) return rc;
+    float ms = 0.f;
+    if ((rc = hlbg_time_steps(ctx, steps_per_trial, &ms))) return rc;
+    if (ms < best_t) {
+      best_t = ms;
+      best = v;
+    }
+  }
+  ctx->sc_variant = best;
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+  ctx->graphs.clear();
+  if (chosen) *chosen = best;
+  if (best_ms) *best_ms = best_t / steps_per_trial;
   return HLBG_OK;
 }
 

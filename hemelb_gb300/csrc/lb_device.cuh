@@ -100,6 +100,7 @@ struct StepArgs {
   int32_t inlet_model, outlet_model;
   double omega, omega_minus;
   float omega_f, omega_minus_f;
+  const double* blk_omega;  // optional [n_blocks * 2]: (omega+, omega-) per block (ensembles)
   float fp16_scale, fp16_inv_scale;
 };
 
@@ -179,7 +180,8 @@ __device__ __forceinline__ double feq64_one(double rho, double mx, double my, do
 }
 
 __device__ __forceinline__ void collide64(const StepArgs& a, const double* f, double& rho,
-                                          double& mx, double& my, double& mz, double* fpost) {
+                                          double& mx, double& my, double& mz, double* fpost,
+                                          double omega, double omega_minus) {
   double r = 0.0, x = 0.0, y = 0.0, z = 0.0;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
@@ -196,15 +198,15 @@ __device__ __forceinline__ void collide64(const StepArgs& a, const double* f, do
   feq64(rho, mx, my, mz, feq);
   if (a.kernel == 0) {
 #pragma unroll
-    for (int i = 0; i < Q; ++i) fpost[i] = f[i] + (f[i] - feq[i]) * a.omega;
+    for (int i = 0; i < Q; ++i) fpost[i] = f[i] + (f[i] - feq[i]) * omega;
   } else {
-    fpost[0] = f[0] + a.omega * (f[0] - feq[0]);
+    fpost[0] = f[0] + omega * (f[0] - feq[0]);
 #pragma unroll
     for (int i = 1; i < Q; i += 2) {
       const int ib = i + 1;
       const double ni = f[i] - feq[i], nb = f[ib] - feq[ib];
-      const double sym = 0.5 * a.omega * (ni + nb);
-      const double asym = 0.5 * a.omega_minus * (ni - nb);
+      const double sym = 0.5 * omega * (ni + nb);
+      const double asym = 0.5 * omega_minus * (ni - nb);
       fpost[i] = f[i] + sym + asym;
       fpost[ib] = f[ib] + sym - asym;
     }
@@ -240,13 +242,14 @@ __device__ __forceinline__ float geq_dev(float dr, float inv_rho, float m2x15, f
 // antisymmetric non-equilibrium parts relax with omega+ and omega- (TRT,
 // Code/lb/kernels/TRT.h:160-188); LBGK is the case omega- = omega+.
 __device__ __forceinline__ void collide_dev(const StepArgs& a, const float* g, float& dr, float& mx,
-                                            float& my, float& mz, float* gpost) {
+                                            float& my, float& mz, float* gpost, float wp_in,
+                                            float wm_in) {
   moments_dev(g, dr, mx, my, mz);
   const float inv_rho = 1.f / (1.f + dr);
   const float A = dr - 1.5f * (mx * mx + my * my + mz * mz) * inv_rho;
   const float c45 = 4.5f * inv_rho;
-  const float wp = a.omega_f;
-  const float wm = a.kernel == 0 ? a.omega_f : a.omega_minus_f;
+  const float wp = wp_in;
+  const float wm = a.kernel == 0 ? wp_in : wm_in;
   gpost[0] = g[0] + wp * (g[0] - weight_f(0) * A);
 #pragma unroll
   for (int i = 1; i < Q; i += 2) {
@@ -260,6 +263,29 @@ __device__ __forceinline__ void collide_dev(const StepArgs& a, const float* g, f
     gpost[i] = g[i] + t + u;
     gpost[i + 1] = g[i + 1] + t - u;
   }
+}
+
+// Relaxation rates of block b: per block for ensembles, else the context's.
+__device__ __forceinline__ void block_rates(const StepArgs& a, int64_t b, double& wp, double& wm) {
+  if (a.blk_omega) {
+    wp = __ldg(a.blk_omega + 2 * b);
+    wm = __ldg(a.blk_omega + 2 * b + 1);
+  } else {
+    wp = a.omega;
+    wm = a.omega_minus;
+  }
+}
+
+template <int P, class T>
+__device__ __forceinline__ void collide_any(const StepArgs& a, int64_t b, const T* f, T& m0, T& mx,
+                                            T& my, T& mz, T* fpost) {
+  double wp, wm;
+  block_rates(a, b, wp, wm);
+  if constexpr (P == 0)
+    collide64(a, f, m0, mx, my, mz, fpost, wp, wm);
+  else
+    collide_dev(a, f, m0, mx, my, mz, fpost, a.blk_omega ? (float)wp : a.omega_f,
+                a.blk_omega ? (float)wm : a.omega_minus_f);
 }
 
 // ---- boundary link values ---------------------------------------------------

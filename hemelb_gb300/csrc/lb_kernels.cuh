@@ -5,13 +5,15 @@
 #include "lb_device.cuh"
 #include "lb_launch.h"
 
+#include <algorithm>
+
 // Launch shape of the stream-and-collide kernel (threads per CTA must divide 512;
 // minimum resident CTAs per SM for the FP32 / FP16 forms and for FP64).
 #ifndef HLBG_SC_THREADS
-#define HLBG_SC_THREADS 256
+#define HLBG_SC_THREADS 128
 #endif
 #ifndef HLBG_SC_MINB
-#define HLBG_SC_MINB 4
+#define HLBG_SC_MINB 10
 #endif
 #ifndef HLBG_SC_MINB64
 #define HLBG_SC_MINB64 2
@@ -189,7 +191,8 @@ template <int P, int D>
 struct PushMixed {
   template <class S, class T, class B>
   static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, int x, int y,
-                                             int z, int l, int64_t own, bool active, uint64_t links,
+                                             int z, int l, int64_t own, bool active, bool row_fluid,
+                                             uint64_t links,
                                              int64_t r, int type, int ioid, const T* fpost, T m0,
                                              T mx, T my, T mz, int64_t b,
                                              const int32_t* __restrict__ block_xyz) {
@@ -202,8 +205,15 @@ struct PushMixed {
     const unsigned lc = (unsigned)((links >> (3 * D)) & 7u);
     int64_t off = nb + D * kSites + tl;
     T v = fpost[D];
-    bool st = active;
-    if (lc != HLBG_LC_PUSH) {
+    bool st = true;
+    if (!active) {
+      // A solid slot is never written by a push nor ever read; a zero there completes
+      // the 32-byte sectors of its row when the row also holds fluid sites (rows
+      // without any receive no write at all and stay untouched).
+      off = own + D * kSites + l;
+      v = (T)0;
+      st = row_fluid;
+    } else if (lc != HLBG_LC_PUSH) {
       if (lc == HLBG_LC_SKIP) {
         st = false;
       } else {
@@ -216,16 +226,16 @@ struct PushMixed {
       }
     }
     if (st) Store<P>::store(fn, off, v, a);
-    PushMixed<P, D + 1>::run(fn, a, base, x, y, z, l, own, active, links, r, type, ioid, fpost, m0,
-                             mx, my, mz, b, block_xyz);
+    PushMixed<P, D + 1>::run(fn, a, base, x, y, z, l, own, active, row_fluid, links, r, type, ioid,
+                             fpost, m0, mx, my, mz, b, block_xyz);
   }
 };
 template <int P>
 struct PushMixed<P, Q> {
   template <class S, class T, class B>
   static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int, int, int, int,
-                                             int64_t, bool, uint64_t, int64_t, int, int, const T*,
-                                             T, T, T, T, int64_t, const int32_t*) {}
+                                             int64_t, bool, bool, uint64_t, int64_t, int, int,
+                                             const T*, T, T, T, T, int64_t, const int32_t*) {}
 };
 
 // ---------------------------------------------------------------------------
@@ -246,10 +256,7 @@ __device__ __forceinline__ void site_update(const StepArgs& a, const B& base,
 #pragma unroll
   for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
   T m0, mx, my, mz;
-  if constexpr (P == 0)
-    collide64(a, f, m0, mx, my, mz, fpost);
-  else
-    collide_dev(a, f, m0, mx, my, mz, fpost);
+  collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
   if (code == 1) {
     PushAll<P, 0>::run(fn, a, base, l >> 6, (l >> 3) & 7, l & 7, fpost);
     return;
@@ -259,22 +266,24 @@ __device__ __forceinline__ void site_update(const StepArgs& a, const B& base,
                          (int)a.b_type[r], a.b_ioid[r], r, fpost, m0, mx, my, mz, block_xyz);
 }
 
-// All slots, one thread each.  A warp covers 32 slots of one block; lanes 0..26
+// One warp's 32 slots of one block (a warp never spans two blocks).  Lanes 0..26
 // hold the block's neighbour table and serve it to the bulk pushes by shuffle, so
 // every lane of a warp with any fluid site stays converged through the pushes.
 template <int P>
-__global__ void __launch_bounds__(HLBG_SC_THREADS, (P == 0 ? HLBG_SC_MINB64 : HLBG_SC_MINB))
-    k_stream_collide(StepArgs a, const int32_t* block_xyz) {
+__device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
+                                             const int32_t* __restrict__ block_xyz) {
   using St = Store<P>;
   using S = typename St::S;
   using T = typename Calc<P>::T;
-  const int64_t s = (int64_t)blockIdx.x * HLBG_SC_THREADS + threadIdx.x;  // < nslot (512 | nslot)
   const int64_t b = s >> 9;
   const int lane = threadIdx.x & 31;
   const int32_t* tab = a.block_nbr + b * 27;
   const int32_t tabreg = lane < 27 ? __ldg(tab + lane) : 0;
   const uint32_t code = a.block_bulk[b] ? 1u : a.site_code[s];
-  if (__ballot_sync(0xffffffffu, code != 0) == 0) return;
+  const unsigned fluid_lanes = __ballot_sync(0xffffffffu, code != 0);
+  if (fluid_lanes == 0) return;
+  // lanes 8r..8r+7 hold one z-row (a 32-byte sector of each direction in FP32)
+  const bool row_fluid = ((fluid_lanes >> (lane & ~7)) & 0xFFu) != 0;
   const int l = (int)(s & (kSites - 1));
   const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + l;
   S* fn = static_cast<S*>(a.f_new);
@@ -287,10 +296,7 @@ __global__ void __launch_bounds__(HLBG_SC_THREADS, (P == 0 ? HLBG_SC_MINB64 : HL
     for (int i = 0; i < Q; ++i) f[i] = (T)(P == 0 ? weight_d(i) : 0.0);
   }
   T m0, mx, my, mz;
-  if constexpr (P == 0)
-    collide64(a, f, m0, mx, my, mz, fpost);
-  else
-    collide_dev(a, f, m0, mx, my, mz, fpost);
+  collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
   const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
   const bool bnd = code >= 2;
   if (__ballot_sync(0xffffffffu, bnd) == 0) {
@@ -300,8 +306,23 @@ __global__ void __launch_bounds__(HLBG_SC_THREADS, (P == 0 ? HLBG_SC_MINB64 : HL
     const uint64_t links = bnd ? a.b_links[r] : 0ull;
     const int type = bnd ? (int)a.b_type[r] : 0;
     const int ioid = bnd ? a.b_ioid[r] : 0;
-    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, l, b * (Q * kSites), code != 0, links, r,
-                         type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
+    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, l, b * (Q * kSites), code != 0, row_fluid,
+                         links, r, type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
+  }
+}
+
+// All slots.  THREADS threads per CTA with at least MINB CTAs resident per SM;
+// PERSIST: a grid of resident CTAs striding over 128-slot chunks in order, else
+// one thread per slot.  The variants are the autotuner's candidates.
+template <int P, int THREADS, int MINB, bool PERSIST>
+__global__ void __launch_bounds__(THREADS, MINB)
+    k_stream_collide(StepArgs a, const int32_t* block_xyz) {
+  if constexpr (!PERSIST) {
+    collide_slot<P>(a, (int64_t)blockIdx.x * THREADS + threadIdx.x, block_xyz);  // 512 | nslot
+  } else {
+    const int64_t nchunk = a.nslot / THREADS;
+    for (int64_t c = blockIdx.x; c < nchunk; c += gridDim.x)
+      collide_slot<P>(a, c * THREADS + threadIdx.x, block_xyz);
   }
 }
 
@@ -340,10 +361,7 @@ __global__ void __launch_bounds__(128) k_iolet_links(StepArgs a, const int32_t* 
 #pragma unroll
   for (int d = 0; d < Q; ++d) f[d] = St::load(fo, d * kSites, a);
   T m0, mx, my, mz;
-  if constexpr (P == 0)
-    collide64(a, f, m0, mx, my, mz, fpost);
-  else
-    collide_dev(a, f, m0, mx, my, mz, fpost);
+  collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
   const uint64_t links = a.b_links[r];
   const int type = a.b_type[r];
   const int ioid = a.b_ioid[r];
@@ -606,7 +624,7 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
       dy = yn / rn - yo / ro;
       dz = zn / rn - zo / ro;
     } else {
-      // deviation form: moments in FP32 on g = f - w, the rest in FP64
+      // deviation form: FP32 on g = f - w; only the mass accumulates in FP64
       float gn[Q], go[Q];
       float mn = 1.0e30f;
 #pragma unroll
@@ -622,10 +640,10 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
       moments_dev(gn, drn, mxn, myn, mzn);
       moments_dev(go, dro, mxo, myo, mzo);
       rn = 1.0 + (double)drn;
-      const double ro = 1.0 + (double)dro;
-      dx = (double)mxn / rn - (double)mxo / ro;
-      dy = (double)myn / rn - (double)myo / ro;
-      dz = (double)mzn / rn - (double)mzo / ro;
+      const float irn = 1.f / (1.f + drn), iro = 1.f / (1.f + dro);
+      dx = (double)(mxn * irn - mxo * iro);
+      dy = (double)(myn * irn - myo * iro);
+      dz = (double)(mzn * irn - mzo * iro);
     }
     acc.bad = bad ? 1ull : 0ull;
     acc.mass = rn;
@@ -658,15 +676,42 @@ static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, in
 
 }  // namespace hlbg
 
+namespace hlbg {
+template <int P, int THREADS, int MINB, bool PERSIST>
+void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
+  unsigned g;
+  if constexpr (PERSIST) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream_collide<P, THREADS, MINB, PERSIST>,
+                                                  THREADS, 0);
+    const int64_t chunks = a.nslot / THREADS;
+    g = (unsigned)std::min<int64_t>(chunks, (int64_t)sms * std::max(per_sm, 1));
+  } else {
+    g = (unsigned)(a.nslot / THREADS);
+  }
+  if (g) k_stream_collide<P, THREADS, MINB, PERSIST><<<g, THREADS, 0, st>>>(a, bxyz);
+}
+}  // namespace hlbg
+
 #define HLBG_INSTANTIATE(P)                                                                     \
   namespace hlbg {                                                                              \
-  void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {     \
+  void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st,      \
+                                 int variant) {                                                 \
     if (a.list) {                                                                               \
       unsigned g = (unsigned)((a.list_count + 255) / 256);                                      \
       if (g) k_stream_collide_list<P><<<g, 256, 0, st>>>(a, bxyz);                              \
-    } else {                                                                                    \
-      unsigned g = (unsigned)((a.nslot + HLBG_SC_THREADS - 1) / HLBG_SC_THREADS);               \
-      if (g) k_stream_collide<P><<<g, HLBG_SC_THREADS, 0, st>>>(a, bxyz);                       \
+      return;                                                                                   \
+    }                                                                                           \
+    if (P == 0) variant = -1;                                                                   \
+    switch (variant) {                                                                          \
+      case 1: launch_sc<P, 128, (P == 0 ? 2 : 8), false>(a, bxyz, st); break;                   \
+      case 2: launch_sc<P, 256, (P == 0 ? 2 : 4), false>(a, bxyz, st); break;                   \
+      case 3: launch_sc<P, 512, (P == 0 ? 1 : 2), false>(a, bxyz, st); break;                   \
+      case 4: launch_sc<P, 128, (P == 0 ? 2 : 10), true>(a, bxyz, st); break;                   \
+      case -1: launch_sc<P, 128, 2, false>(a, bxyz, st); break;                                 \
+      default: launch_sc<P, HLBG_SC_THREADS, HLBG_SC_MINB, false>(a, bxyz, st); break;          \
     }                                                                                           \
   }                                                                                             \
   void launch_iolet_links_##P(const StepArgs& a, const int32_t* rec, const int32_t* rec_slot,    \

@@ -9,6 +9,11 @@ namespace hlbg {
 
 struct StepArgs;
 
+// Launch variants of the stream-and-collide kernel (FP32 / FP16 forms; FP64 has one):
+// 0 default shape, 1: 128x8, 2: 256x4, 3: 512x2 threads x resident CTAs per SM,
+// 4: persistent 128-thread CTAs striding over the slots.
+constexpr int kSCVariants = 5;
+
 struct PostArgs {
   void* f_new;
   int64_t stride;
@@ -66,7 +71,8 @@ struct MonitorArgs {
 };
 
 #define HLBG_DECLARE(P)                                                              \
-  void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st); \
+  void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st,  \
+                                 int variant);                                           \
   void launch_iolet_links_##P(const StepArgs& a, const int32_t* rec, const int32_t* rec_slot, \
                               int64_t n, const int32_t* bxyz, cudaStream_t st);          \
   void launch_post_step_##P(const PostArgs& p, cudaStream_t st);                     \

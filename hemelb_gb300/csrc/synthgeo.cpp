@@ -123,6 +123,11 @@ struct Geometry {
   std::vector<float> cuts;
   int64_t n_fluid = 0;
   bool with_cuts = false;
+  // ensemble: member of each output block and per-member parameters
+  std::vector<int32_t> block_member;
+  std::vector<double> member_tau;
+  std::vector<double> member_shape;  // radius, length, narrowing per member
+  std::vector<int64_t> member_sites;
 };
 
 uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
@@ -573,6 +578,131 @@ int hlbg_synth_tree(uint64_t seed, int32_t box_sites, int32_t n_roots, int32_t d
   }
   place(*g, box_sites);
   return finish(g, n_threads, handle);
+}
+
+int hlbg_synth_ensemble(uint64_t seed, int32_t n_members, int32_t q, int32_t n_threads,
+                        void** handle) {
+  // Seeded stenosed pipes: radius U[6,20], length U[60,240], Gaussian narrowing
+  // U[0,0.7] of the radius, tau U[0.55,1.0].  Each member occupies its own cell of
+  // blocks in a 2-D arrangement over (x, y), cells separated by one empty block so
+  // that no link joins two members.  Inlet i / outlet i belong to member i.
+  if (!handle || n_members < 1 || n_members > 65536 || (q != 15 && q != 19)) return HLBG_ERR_INVAL;
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  auto* g = new Geometry();
+  g->q = q;
+  g->with_cuts = true;
+  const int cell_xy = 6;   // blocks: 2 * 20 + margins fits in 5 blocks, plus a 1-block gap
+  const int cell_z = 32;   // blocks: length <= 240 + margins fits in 31, plus a gap
+  const int side = (int)std::ceil(std::sqrt((double)n_members));
+  std::vector<std::unique_ptr<Geometry>> members;
+  for (int m = 0; m < n_members; ++m) {
+    double R = 6.0 + 14.0 * U(rng);
+    int L = 60 + (int)std::floor(181.0 * U(rng));
+    double depth = 0.7 * U(rng);
+    double tau = 0.55 + 0.45 * U(rng);
+    auto mg = std::make_unique<Geometry>();
+    mg->q = q;
+    mg->with_cuts = true;
+    Shape sh{};
+    sh.kind = 1;
+    sh.a = {0, 0, -0.5};
+    sh.b = {0, 0, L + 0.5};
+    sh.r = R;
+    sh.depth = depth;
+    sh.zc = 0.5 * L;
+    sh.sigma = std::max(2.0, R);
+    mg->shapes.push_back(sh);
+    mg->inlets.push_back(mk_iolet(0, m, {0, 0, -0.5}, {0, 0, 1}, R));
+    mg->outlets.push_back(mk_iolet(1, m, {0, 0, L + 0.5}, {0, 0, -1}, R));
+    // centre the pipe in its cell: axis at 8*cell_xy/2 - 4 sites from the cell corner
+    Vec off{(double)(cell_xy * 8 / 2 - 4), (double)(cell_xy * 8 / 2 - 4), 3.0};
+    for (auto& sp : mg->shapes) {
+      sp.a = add(sp.a, off);
+      sp.b = add(sp.b, off);
+      sp.zc += off.z;
+    }
+    for (auto* v : {&mg->inlets, &mg->outlets})
+      for (auto& io : *v) io.pos = add(io.pos, off);
+    mg->nb[0] = mg->nb[1] = cell_xy - 1;
+    mg->nb[2] = cell_z - 1;
+    for (auto& sp : mg->shapes) shape_bounds(sp);
+    for (auto* v : {&mg->inlets, &mg->outlets})
+      for (auto& io : *v) iolet_bounds(io);
+    g->member_tau.push_back(tau);
+    g->member_shape.push_back(R);
+    g->member_shape.push_back((double)L);
+    g->member_shape.push_back(depth);
+    members.push_back(std::move(mg));
+  }
+  // voxelise members in parallel
+  std::atomic<int> next{0};
+  if (n_threads <= 0) n_threads = (int)std::max(1u, std::thread::hardware_concurrency());
+  auto work = [&]() {
+    for (;;) {
+      int m = next.fetch_add(1);
+      if (m >= n_members) break;
+      voxelize(*members[m], 1);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < n_threads; ++t) th.emplace_back(work);
+  work();
+  for (auto& t : th) t.join();
+  g->nb[0] = side * cell_xy;
+  g->nb[1] = side * cell_xy;
+  g->nb[2] = cell_z;
+  const int nl = q - 1;
+  for (int m = 0; m < n_members; ++m) {
+    Geometry& mg = *members[m];
+    const int ox = (m % side) * cell_xy, oy = (m / side) * cell_xy;
+    const int64_t b0 = (int64_t)g->block_coords.size() / 3;
+    const int64_t nbm = (int64_t)mg.block_coords.size() / 3;
+    for (int64_t b = 0; b < nbm; ++b) {
+      g->block_coords.push_back(mg.block_coords[3 * b] + ox);
+      g->block_coords.push_back(mg.block_coords[3 * b + 1] + oy);
+      g->block_coords.push_back(mg.block_coords[3 * b + 2]);
+      g->block_member.push_back(m);
+    }
+    g->fluid_mask.insert(g->fluid_mask.end(), mg.fluid_mask.begin(), mg.fluid_mask.end());
+    for (size_t r = 0; r < mg.link_site.size(); ++r) {
+      g->link_site.push_back(mg.link_site[r] + b0 * kSitesPerBlock);
+      g->wall_mask.push_back(mg.wall_mask[r]);
+      g->iolet_mask.push_back(mg.iolet_mask[r]);
+      g->iolet_id.push_back(mg.iolet_id[r] >= 0 ? m : -1);
+      g->site_type.push_back(mg.site_type[r]);
+    }
+    g->cuts.insert(g->cuts.end(), mg.cuts.begin(), mg.cuts.end());
+    g->n_fluid += mg.n_fluid;
+    g->member_sites.push_back(mg.n_fluid);
+    Vec shift{8.0 * ox, 8.0 * oy, 0.0};
+    for (auto io : mg.inlets) {
+      io.pos = add(io.pos, shift);
+      io.index = m;
+      g->inlets.push_back(io);
+    }
+    for (auto io : mg.outlets) {
+      io.pos = add(io.pos, shift);
+      io.index = m;
+      g->outlets.push_back(io);
+    }
+  }
+  (void)nl;
+  *handle = g;
+  return HLBG_OK;
+}
+
+int hlbg_synth_members(void* handle, int32_t* n_members, const int32_t** block_member,
+                       const double** member_tau, const double** member_shape,
+                       const int64_t** member_sites) {
+  if (!handle) return HLBG_ERR_INVAL;
+  auto* g = static_cast<Geometry*>(handle);
+  if (n_members) *n_members = (int32_t)g->member_tau.size();
+  if (block_member) *block_member = g->block_member.empty() ? nullptr : g->block_member.data();
+  if (member_tau) *member_tau = g->member_tau.empty() ? nullptr : g->member_tau.data();
+  if (member_shape) *member_shape = g->member_shape.empty() ? nullptr : g->member_shape.data();
+  if (member_sites) *member_sites = g->member_sites.empty() ? nullptr : g->member_sites.data();
+  return HLBG_OK;
 }
 
 int hlbg_synth_view(void* handle, hlbg_geometry* out, int64_t* n_fluid, int32_t* n_in,

@@ -99,6 +99,28 @@ class SyntheticGeometry:
         return cls(h, lib)
 
     @classmethod
+    def ensemble(cls, seed=2024, n_members=512, q=19, n_threads=0):
+        lib = capi.load()
+        h = C.c_void_p()
+        check(lib.hlbg_synth_ensemble(seed, n_members, q, n_threads, C.byref(h)))
+        return cls(h, lib)
+
+    def members(self):
+        """(block_member[n_blocks], member_tau[m], member_shape[m,3], member_sites[m]) or None."""
+        n = C.c_int32()
+        bm = C.POINTER(C.c_int32)()
+        tau = C.POINTER(C.c_double)()
+        shape = C.POINTER(C.c_double)()
+        sites = C.POINTER(C.c_int64)()
+        check(self._lib.hlbg_synth_members(self._h, C.byref(n), C.byref(bm), C.byref(tau),
+                                           C.byref(shape), C.byref(sites)))
+        if n.value == 0:
+            return None
+        m = n.value
+        return (_np(bm, self.n_blocks, np.int32).copy(), _np(tau, m, np.float64).copy(),
+                _np(shape, 3 * m, np.float64).reshape(m, 3).copy(), _np(sites, m, np.int64).copy())
+
+    @classmethod
     def tree(cls, seed=7, box_sites=1280, n_roots=1, depth=7, root_radius=60.0, q=19,
              with_cuts=False, n_threads=0):
         lib = capi.load()
@@ -227,6 +249,21 @@ class LBM:
         check(self._lib.hlbg_step(self._ctx, n, None), self._ctx)
         if sync:
             check(self._lib.hlbg_sync(self._ctx), self._ctx)
+
+    def DoTimeStepGraph(self, n: int = 1, sync: bool = True):
+        check(self._lib.hlbg_step_graph(self._ctx, n), self._ctx)
+        if sync:
+            check(self._lib.hlbg_sync(self._ctx), self._ctx)
+
+    def autotune(self, steps_per_trial: int = 5):
+        v = C.c_int32()
+        ms = C.c_float()
+        check(self._lib.hlbg_autotune(self._ctx, steps_per_trial, C.byref(v), C.byref(ms)), self._ctx)
+        return int(v.value), float(ms.value)
+
+    def SetBlockTau(self, tau_per_block: np.ndarray):
+        t = np.ascontiguousarray(tau_per_block, dtype=np.float64)
+        check(self._lib.hlbg_set_block_tau(self._ctx, t.ctypes.data_as(_D)), self._ctx)
 
     def StreamAndCollide(self, first: int, count: int):
         check(self._lib.hlbg_stream_and_collide_range(self._ctx, first, count), self._ctx)

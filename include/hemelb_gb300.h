@@ -150,6 +150,18 @@ int hlbg_synth_stenosis(double radius, int32_t length, double depth, int32_t q,
 int hlbg_synth_tree(uint64_t seed, int32_t box_sites, int32_t n_roots, int32_t depth,
                     double root_radius, int32_t q, int32_t with_cuts, int32_t n_threads,
                     void **geom_handle);
+/* Ensemble of n seeded stenosed pipes (radius 6-20, length 60-240, Gaussian
+ * narrowing 0-70%, tau 0.55-1.0) packed into one sparse geometry, one member per
+ * cell of blocks with empty blocks between members; inlet m and outlet m belong
+ * to member m. */
+int hlbg_synth_ensemble(uint64_t seed, int32_t n_members, int32_t q, int32_t n_threads,
+                        void **geom_handle);
+/* Members of an ensemble: member of each block (in hlbg_geometry block order),
+ * per-member tau, shape (radius, length, narrowing) and fluid-site counts (NULL
+ * for a single geometry). */
+int hlbg_synth_members(void *geom_handle, int32_t *n_members, const int32_t **block_member,
+                       const double **member_tau, const double **member_shape,
+                       const int64_t **member_sites);
 /* Access the generated geometry and its iolets (pointers stay owned by the handle). */
 int hlbg_synth_view(void *geom_handle, hlbg_geometry *out, int64_t *n_fluid_sites,
                     int32_t *n_inlets, int32_t *n_outlets);
@@ -185,6 +197,18 @@ int hlbg_init_equilibrium_field(hlbg_ctx *ctx, const double *rho, const double *
  * Returns after enqueueing; hlbg_sync waits. */
 int hlbg_step(hlbg_ctx *ctx, int32_t nsteps, void *cuda_stream);
 int hlbg_sync(hlbg_ctx *ctx);
+/* Same as hlbg_step, as CUDA graph launches: every kernel of up to 1024 steps is
+ * captured once per step count and replayed (launch-bound small geometries and
+ * batched ensembles). */
+int hlbg_step_graph(hlbg_ctx *ctx, int32_t nsteps);
+/* Autotuner: time each launch shape / schedule of the stream-and-collide kernel
+ * (threads per CTA x resident CTAs per SM, per-slot grid or persistent grid) on
+ * this context for steps_per_trial steps and keep the fastest.  Advances the
+ * state like hlbg_step.  chosen / best_ms may be NULL. */
+int hlbg_autotune(hlbg_ctx *ctx, int32_t steps_per_trial, int32_t *chosen, float *best_ms);
+/* Per-block relaxation time (input block order), e.g. one tau per ensemble member;
+ * omega = -1/tau per block (LbmParameters::CalcDerivedParams). */
+int hlbg_set_block_tau(hlbg_ctx *ctx, const double *tau_per_block);
 
 /* Per-range drop-in for one streamer: ranges are contiguous site ids. */
 int hlbg_stream_and_collide_range(hlbg_ctx *ctx, int64_t first, int64_t count);
