@@ -63,7 +63,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--members", type=int, default=512)
-    ap.add_argument("--report", default=None, choices=["precision", "steady", "ensemble"],
+    ap.add_argument("--report", default=None, choices=["precision", "steady", "ensemble", "tree_precision"],
                     help="print a report instead of the throughput line")
     return ap.parse_args()
 
@@ -264,6 +264,9 @@ def main():
         from hemelb_gb300 import cases, reports
         if args.report == "precision":
             print(json.dumps(reports.precision_report(steps=args.steps)), flush=True)
+        elif args.report == "tree_precision":
+            print(json.dumps(reports.tree_precision_report(steps=args.steps, roots=args.roots,
+                                                           box=args.box, depth=args.depth)), flush=True)
         elif args.report == "ensemble":
             print(json.dumps(reports.ensemble_report(args.members, steps=args.steps,
                                                      warmup=args.warmup)), flush=True)

@@ -63,10 +63,12 @@ def build(force: bool = False, verbose: bool = False, defines=(), out: str | Non
         objs.append(obj)
         jobs.append([NVCC] + ARCH + COMMON + extra + ["-D" + d for d in defines]
                     + ["-c", os.path.join(SRC, unit), "-o", obj])
+    zlib = os.path.exists("/usr/include/zlib.h")  # .gmy reader needs zlib
     for unit in HOST_UNITS:
         obj = os.path.join(bdir, unit + ".o")
         objs.append(obj)
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
+                     "-DHLBG_HAVE_ZLIB=%d" % int(zlib),
                      "-I", os.path.join(HERE, "..", "include"), "-c",
                      os.path.join(SRC, unit), "-o", obj])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
@@ -75,7 +77,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), out: str | Non
         for o in outs:
             sys.stdout.write(o)
     tmp = lib + ".tmp"
-    _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
+    _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"] + (["-lz"] if zlib else []))
     os.replace(tmp, lib)
     return lib
 

@@ -73,6 +73,8 @@ SIGNATURES = {
     "hlbg_synth_members": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.POINTER(C.c_int32)),
                                      C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.POINTER(C.c_double)),
                                      C.POINTER(C.POINTER(C.c_int64))]),
+    "hlbg_write_gmy": (C.c_int, [C.POINTER(Geometry), C.c_char_p]),
+    "hlbg_read_gmy": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "hlbg_synth_view": (C.c_int, [C.c_void_p, C.POINTER(Geometry), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "hlbg_synth_iolet": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double * 3, C.c_double * 3,

@@ -118,11 +118,21 @@ struct Store<0> {
     p[i] = v;
   }
 };
+// Distributions of the old array are read exactly once per step: the streaming
+// hint (ld.global.cs) keeps them from displacing the partially written sectors of
+// the new array in L2.
+#ifndef HLBG_STREAM_LOADS
+#define HLBG_STREAM_LOADS 1
+#endif
 template <>
 struct Store<1> {
   using S = float;
   static __device__ __forceinline__ float load(const S* p, int64_t i, const StepArgs&) {
+#if HLBG_STREAM_LOADS
+    return __ldcs(p + i);
+#else
     return __ldg(p + i);
+#endif
   }
   static __device__ __forceinline__ void store(S* p, int64_t i, float v, const StepArgs&) {
     p[i] = v;
@@ -132,7 +142,11 @@ template <>
 struct Store<2> {
   using S = __half;
   static __device__ __forceinline__ float load(const S* p, int64_t i, const StepArgs& a) {
+#if HLBG_STREAM_LOADS
+    return __half2float(__ldcs(p + i)) * a.fp16_inv_scale;
+#else
     return __half2float(__ldg(p + i)) * a.fp16_inv_scale;
+#endif
   }
   static __device__ __forceinline__ void store(S* p, int64_t i, float v, const StepArgs& a) {
     p[i] = __float2half_rn(v * a.fp16_scale);

@@ -30,6 +30,11 @@
 #include <thread>
 #include <vector>
 
+#if HLBG_HAVE_ZLIB
+#include <zlib.h>
+#endif
+#include <cstdio>
+
 #include "../../include/hemelb_gb300.h"
 
 namespace {
@@ -703,6 +708,327 @@ int hlbg_synth_members(void* handle, int32_t* n_members, const int32_t** block_m
   if (member_shape) *member_shape = g->member_shape.empty() ? nullptr : g->member_shape.data();
   if (member_sites) *member_sites = g->member_sites.empty() ? nullptr : g->member_sites.data();
   return HLBG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// HemeLB .gmy geometry files (doc/dev/file-formats/geometry.md; the reader of the
+// reference is Code/geometry/GeometryReader.cc:80-166 and ParseSite :556-657).
+// XDR big-endian words: preamble (magics 0x686c6221 / 0x676d7904, version 4,
+// block counts, block size, pad), one (fluid sites, compressed bytes,
+// uncompressed bytes) header per block with z fastest, then the zlib-compressed
+// site records of every non-empty block, sites with z fastest.  A fluid site
+// carries 26 links over the Moore neighbourhood in lexicographic (x, y, z)
+// order without the rest vector: cut type (0 none, 1 wall, 2 inlet, 3 outlet),
+// then an iolet index for inlets/outlets and a float cut distance for all but
+// none; then a wall-normal flag and, if set, the normal.
+// ---------------------------------------------------------------------------
+namespace {
+struct XdrIn {
+  const uint8_t* p;
+  size_t n, at = 0;
+  bool ok = true;
+  uint32_t u32() {
+    if (at + 4 > n) {
+      ok = false;
+      return 0;
+    }
+    uint32_t v = ((uint32_t)p[at] << 24) | ((uint32_t)p[at + 1] << 16) | ((uint32_t)p[at + 2] << 8) |
+                 (uint32_t)p[at + 3];
+    at += 4;
+    return v;
+  }
+  float f32() {
+    uint32_t v = u32();
+    float f;
+    std::memcpy(&f, &v, 4);
+    return f;
+  }
+};
+}  // namespace
+
+extern "C" {
+int hlbg_read_gmy(const char* path, int32_t q, void** handle) {
+  if (!path || !handle || (q != 15 && q != 19)) return HLBG_ERR_INVAL;
+#if !HLBG_HAVE_ZLIB
+  (void)path;
+  return HLBG_ERR_STATE;  // built without zlib
+#else
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return HLBG_ERR_INVAL;
+  std::vector<uint8_t> file;
+  {
+    uint8_t buf[1 << 16];
+    size_t r;
+    while ((r = std::fread(buf, 1, sizeof(buf), fp)) > 0) file.insert(file.end(), buf, buf + r);
+    std::fclose(fp);
+  }
+  XdrIn in{file.data(), file.size()};
+  const uint32_t m1 = in.u32(), m2 = in.u32(), ver = in.u32();
+  const uint32_t nbx = in.u32(), nby = in.u32(), nbz = in.u32(), bs = in.u32();
+  in.u32();
+  if (!in.ok || m1 != 0x686c6221u || m2 != 0x676d7904u || ver != 4 || bs == 0 || bs > 64)
+    return HLBG_ERR_INVAL;
+  const uint64_t nblk = (uint64_t)nbx * nby * nbz;
+  std::vector<uint32_t> hdr(nblk * 3);
+  for (auto& h : hdr) h = in.u32();
+  if (!in.ok) return HLBG_ERR_INVAL;
+  // lattice direction of each of the 26 Moore links (0 = not in the lattice)
+  const int* cx = q == 15 ? CX15 : CX19;
+  const int* cy = q == 15 ? CY15 : CY19;
+  const int* cz = q == 15 ? CZ15 : CZ19;
+  int link_dir[26];
+  {
+    int i = 0;
+    for (int dx = -1; dx <= 1; ++dx)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dz = -1; dz <= 1; ++dz) {
+          if (!dx && !dy && !dz) continue;
+          link_dir[i] = 0;
+          for (int d = 1; d < q; ++d)
+            if (cx[d] == dx && cy[d] == dy && cz[d] == dz) link_dir[i] = d;
+          ++i;
+        }
+  }
+  struct SiteRec {
+    int64_t x, y, z;
+    uint32_t wall, iolet;
+    int32_t ioid;
+    int8_t type;
+    float cut[26];
+  };
+  std::vector<SiteRec> sites;
+  size_t off = in.at;
+  std::vector<uint8_t> raw;
+  for (uint64_t b = 0; b < nblk; ++b) {
+    const uint32_t nsite = hdr[3 * b], clen = hdr[3 * b + 1], ulen = hdr[3 * b + 2];
+    if (nsite == 0) continue;
+    if (off + clen > file.size()) return HLBG_ERR_INVAL;
+    raw.assign(ulen, 0);
+    uLongf got = ulen;
+    if (uncompress(raw.data(), &got, file.data() + off, clen) != Z_OK || got != ulen) return HLBG_ERR_INVAL;
+    off += clen;
+    const int64_t bx = (int64_t)(b / ((uint64_t)nby * nbz)), by = (int64_t)((b / nbz) % nby),
+                  bz = (int64_t)(b % nbz);
+    XdrIn s{raw.data(), raw.size()};
+    uint32_t seen = 0;
+    for (uint32_t lx = 0; lx < bs; ++lx)
+      for (uint32_t ly = 0; ly < bs; ++ly)
+        for (uint32_t lz = 0; lz < bs; ++lz) {
+          const uint32_t fluid = s.u32();
+          if (!s.ok || fluid > 1) return HLBG_ERR_INVAL;
+          if (!fluid) continue;
+          SiteRec r{};
+          r.x = bx * bs + lx;
+          r.y = by * bs + ly;
+          r.z = bz * bs + lz;
+          r.ioid = -1;
+          bool had_in = false, had_out = false, any_wall = false;
+          for (int d = 0; d < 26; ++d) r.cut[d] = -1.0f;  // GeometrySiteLink default
+          for (int i = 0; i < 26; ++i) {
+            const uint32_t type = s.u32();
+            int32_t io = -1;
+            float dist = -1.0f;
+            if (type == 1) {
+              dist = s.f32();
+              any_wall = true;
+            } else if (type == 2 || type == 3) {
+              io = (int32_t)s.u32();
+              dist = s.f32();
+            } else if (type != 0) {
+              return HLBG_ERR_INVAL;
+            }
+            const int d = link_dir[i];
+            if (d == 0) continue;  // link not in this lattice
+            r.cut[d - 1] = dist;
+            if (type == 1) r.wall |= 1u << (d - 1);
+            if (type == 2 || type == 3) {
+              r.iolet |= 1u << (d - 1);
+              r.ioid = io;  // SiteData: the last iolet link in direction order wins
+              if (type == 2) had_in = true; else had_out = true;
+            }
+          }
+          const uint32_t has_normal = s.u32();
+          if (has_normal > 1 || (has_normal == 1) != any_wall) return HLBG_ERR_INVAL;
+          if (has_normal) {
+            s.f32();
+            s.f32();
+            s.f32();
+          }
+          if (!s.ok) return HLBG_ERR_INVAL;
+          r.type = had_in ? HLBG_SITE_INLET : (had_out ? HLBG_SITE_OUTLET : HLBG_SITE_FLUID);
+          sites.push_back(r);
+          ++seen;
+        }
+    if (seen != nsite) return HLBG_ERR_INVAL;
+  }
+  // re-block into 8^3 blocks, listed in Morton order
+  auto* g = new Geometry();
+  g->q = q;
+  g->with_cuts = true;
+  int64_t ext[3] = {(int64_t)nbx * bs, (int64_t)nby * bs, (int64_t)nbz * bs};
+  for (int a = 0; a < 3; ++a) g->nb[a] = (int)((ext[a] + kBlock - 1) / kBlock);
+  std::vector<std::pair<uint64_t, size_t>> order;
+  order.reserve(sites.size());
+  for (size_t i = 0; i < sites.size(); ++i) {
+    const auto& r = sites[i];
+    uint64_t key = (morton3((uint32_t)(r.x >> 3), (uint32_t)(r.y >> 3), (uint32_t)(r.z >> 3)) << 9) |
+                   (uint64_t)(((r.x & 7) * 8 + (r.y & 7)) * 8 + (r.z & 7));
+    order.push_back({key, i});
+  }
+  std::sort(order.begin(), order.end());
+  uint64_t cur_block = ~0ull;
+  int64_t bi = -1;
+  for (auto& [key, i] : order) {
+    const auto& r = sites[i];
+    const uint64_t blk = key >> 9;
+    if (blk != cur_block) {
+      cur_block = blk;
+      ++bi;
+      g->block_coords.push_back((int32_t)(r.x >> 3));
+      g->block_coords.push_back((int32_t)(r.y >> 3));
+      g->block_coords.push_back((int32_t)(r.z >> 3));
+      for (int w = 0; w < 8; ++w) g->fluid_mask.push_back(0);
+    }
+    const int l = (int)(key & 511);
+    g->fluid_mask[bi * 8 + l / 64] |= 1ull << (l % 64);
+    g->n_fluid++;
+    if (r.wall || r.iolet) {
+      g->link_site.push_back(bi * kSitesPerBlock + l);
+      g->wall_mask.push_back(r.wall);
+      g->iolet_mask.push_back(r.iolet);
+      g->iolet_id.push_back(r.ioid);
+      g->site_type.push_back(r.type);
+      for (int d = 0; d < q - 1; ++d) g->cuts.push_back(r.cut[d]);
+    }
+  }
+  *handle = g;
+  return HLBG_OK;
+#endif
+}
+}  // extern "C"
+
+int hlbg_write_gmy(const hlbg_geometry* g, const char* path) {
+  // Inverse of hlbg_read_gmy with 8^3 blocks.  Lattice links keep their cut type,
+  // iolet index and distance; Moore links outside the lattice are written as
+  // NONE.  Sites with a wall link get a wall normal (the normalised sum of their
+  // wall-link vectors), as the format requires one exactly for wall sites.
+#if !HLBG_HAVE_ZLIB
+  (void)g;
+  (void)path;
+  return HLBG_ERR_STATE;
+#else
+  if (!g || !path || (g->q != 15 && g->q != 19) || g->block_size != 8) return HLBG_ERR_INVAL;
+  const int q = g->q;
+  const int* cx = q == 15 ? CX15 : CX19;
+  const int* cy = q == 15 ? CY15 : CY19;
+  const int* cz = q == 15 ? CZ15 : CZ19;
+  int dir_of_link[26];
+  {
+    int i = 0;
+    for (int dx = -1; dx <= 1; ++dx)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dz = -1; dz <= 1; ++dz) {
+          if (!dx && !dy && !dz) continue;
+          dir_of_link[i] = 0;
+          for (int d = 1; d < q; ++d)
+            if (cx[d] == dx && cy[d] == dy && cz[d] == dz) dir_of_link[i] = d;
+          ++i;
+        }
+  }
+  const uint64_t NX = g->blocks[0], NY = g->blocks[1], NZ = g->blocks[2];
+  std::vector<int64_t> idx(NX * NY * NZ, -1);
+  for (int64_t b = 0; b < g->n_blocks; ++b)
+    idx[((uint64_t)g->block_coords[3 * b] * NY + g->block_coords[3 * b + 1]) * NZ + g->block_coords[3 * b + 2]] = b;
+  std::vector<int64_t> rec_of(g->n_blocks * 512, -1);
+  for (int64_t r = 0; r < g->n_link_sites; ++r) rec_of[g->link_site[r]] = r;
+  auto put = [](std::vector<uint8_t>& v, uint32_t w) {
+    v.push_back((uint8_t)(w >> 24));
+    v.push_back((uint8_t)(w >> 16));
+    v.push_back((uint8_t)(w >> 8));
+    v.push_back((uint8_t)w);
+  };
+  auto putf = [&](std::vector<uint8_t>& v, float f) {
+    uint32_t w;
+    std::memcpy(&w, &f, 4);
+    put(v, w);
+  };
+  std::vector<uint8_t> head, body;
+  put(head, 0x686c6221u);
+  put(head, 0x676d7904u);
+  put(head, 4u);
+  put(head, (uint32_t)NX);
+  put(head, (uint32_t)NY);
+  put(head, (uint32_t)NZ);
+  put(head, 8u);
+  put(head, 0u);
+  std::vector<uint8_t> raw;
+  for (uint64_t gb = 0; gb < NX * NY * NZ; ++gb) {
+    const int64_t b = idx[gb];
+    if (b < 0) {
+      put(head, 0u);
+      put(head, 0u);
+      put(head, 0u);
+      continue;
+    }
+    raw.clear();
+    uint32_t nfluid = 0;
+    for (int l = 0; l < 512; ++l) {
+      const bool fl = (g->fluid_mask[b * 8 + l / 64] >> (l % 64)) & 1ull;
+      put(raw, fl ? 1u : 0u);
+      if (!fl) continue;
+      ++nfluid;
+      const int64_t r = rec_of[b * 512 + l];
+      double nx = 0, ny = 0, nz = 0;
+      bool any_wall = false;
+      for (int i = 0; i < 26; ++i) {
+        const int d = dir_of_link[i];
+        uint32_t type = 0;
+        if (d && r >= 0) {
+          const bool w = (g->wall_mask[r] >> (d - 1)) & 1u, io = (g->iolet_mask[r] >> (d - 1)) & 1u;
+          const float dist = g->cut_distance ? g->cut_distance[r * (q - 1) + d - 1] : 0.5f;
+          if (io) {
+            type = g->site_type[r] == HLBG_SITE_OUTLET ? 3u : 2u;
+            put(raw, type);
+            put(raw, (uint32_t)std::max(0, g->iolet_id[r]));
+            putf(raw, dist);
+            continue;
+          }
+          if (w) {
+            put(raw, 1u);
+            putf(raw, dist);
+            any_wall = true;
+            nx += cx[d];
+            ny += cy[d];
+            nz += cz[d];
+            continue;
+          }
+        }
+        put(raw, 0u);
+      }
+      put(raw, any_wall ? 1u : 0u);
+      if (any_wall) {
+        double m = std::sqrt(nx * nx + ny * ny + nz * nz);
+        if (m == 0) m = 1;
+        putf(raw, (float)(nx / m));
+        putf(raw, (float)(ny / m));
+        putf(raw, (float)(nz / m));
+      }
+    }
+    uLongf clen = compressBound(raw.size());
+    std::vector<uint8_t> comp(clen);
+    if (compress(comp.data(), &clen, raw.data(), raw.size()) != Z_OK) return HLBG_ERR_INVAL;
+    put(head, nfluid);
+    put(head, (uint32_t)clen);
+    put(head, (uint32_t)raw.size());
+    body.insert(body.end(), comp.begin(), comp.begin() + clen);
+  }
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return HLBG_ERR_INVAL;
+  bool ok = std::fwrite(head.data(), 1, head.size(), fp) == head.size() &&
+            std::fwrite(body.data(), 1, body.size(), fp) == body.size();
+  ok = (std::fclose(fp) == 0) && ok;
+  return ok ? HLBG_OK : HLBG_ERR_INVAL;
+#endif
 }
 
 int hlbg_synth_view(void* handle, hlbg_geometry* out, int64_t* n_fluid, int32_t* n_in,

@@ -56,6 +56,10 @@ class SyntheticGeometry:
         self.cut_distance = (_np(v.cut_distance, n * (v.q - 1), np.float32).reshape(n, v.q - 1)
                              if v.cut_distance else None)
 
+    def write_gmy(self, path: str):
+        """Write this geometry as a HemeLB .gmy file (readable by GeometryReader)."""
+        check(self._lib.hlbg_write_gmy(C.byref(self.view), path.encode()), None, "hlbg_write_gmy")
+
     def iolet(self, is_outlet: bool, index: int):
         pos = (C.c_double * 3)()
         nrm = (C.c_double * 3)()
@@ -96,6 +100,14 @@ class SyntheticGeometry:
         lib = capi.load()
         h = C.c_void_p()
         check(lib.hlbg_synth_stenosis(radius, length, depth, q, int(with_cuts), C.byref(h)))
+        return cls(h, lib)
+
+    @classmethod
+    def from_gmy(cls, path: str, q: int = 19):
+        """A HemeLB .gmy file (GeometryReader's input) as a sparse block geometry."""
+        lib = capi.load()
+        h = C.c_void_p()
+        check(lib.hlbg_read_gmy(path.encode(), q, C.byref(h)), None, "hlbg_read_gmy(%s)" % path)
         return cls(h, lib)
 
     @classmethod

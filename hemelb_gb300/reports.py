@@ -131,3 +131,30 @@ def ensemble_report(n_members: int = 512, steps: int = 50, warmup: int = 5, seed
                         "setup_s": t_setup, "stable": bool(st.unstable_sites == 0)},
             "sequential": {"mlups": seq_sites * steps / seq_s / 1e6, "seconds": seq_s},
             "speedup": (n * steps / batched_s) / (seq_sites * steps / seq_s)}
+
+
+def tree_precision_report(steps: int = 1000, roots: int = 5, box: int = 1280, depth: int = 7) -> dict:
+    """The forest workload (TRT, SBB, Nash) in FP64, FP32-deviation and FP16-storage
+    forms from rest for `steps` steps; velocity / pressure error of the reduced forms
+    against FP64 (FP64 is the oracle's arithmetic, bit-exact on the GPU)."""
+    case = cases.tree(n_roots=roots, box_sites=box, depth=depth, precision=capi.FP64)
+    out = {"workload": "forest of %d trees depth %d in %d^3, %d fluid sites, %d steps from rest, TRT"
+                       % (roots, depth, box, case.geometry.n_fluid, steps), "forms": {}}
+    ref = None
+    for name, prec in (("fp64", capi.FP64), ("fp32dev", capi.FP32DEV), ("fp16", capi.FP16)):
+        s = case.solver(prec)
+        s.SetInitialConditions()
+        t0 = time.perf_counter()
+        s.DoTimeStep(steps)
+        dt = time.perf_counter() - t0
+        rho, u = s.macro()
+        s.close()
+        entry = {"seconds": dt, "mlups": len(rho) * steps / dt / 1e6}
+        if ref is None:
+            ref = (rho, u)
+            entry["u_peak"] = float(np.linalg.norm(u, axis=1).max())
+        else:
+            entry.update(_errors(rho, u, *ref))
+        out["forms"][name] = entry
+        del rho, u
+    return out

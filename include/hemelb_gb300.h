@@ -162,6 +162,15 @@ int hlbg_synth_ensemble(uint64_t seed, int32_t n_members, int32_t q, int32_t n_t
 int hlbg_synth_members(void *geom_handle, int32_t *n_members, const int32_t **block_member,
                        const double **member_tau, const double **member_shape,
                        const int64_t **member_sites);
+/* Read a HemeLB .gmy geometry file (version 4) for lattice q into a geometry
+ * handle (sites re-blocked into 8^3 blocks whatever the file's block size).
+ * The file carries no iolet positions: the caller supplies iolets in lattice
+ * units.  HLBG_ERR_STATE if the library was built without zlib. */
+int hlbg_read_gmy(const char *path, int32_t q, void **geom_handle);
+/* Write a sparse block geometry as a HemeLB .gmy file (version 4, 8^3 blocks);
+ * lattice links keep type, iolet index and cut distance, other Moore links are
+ * NONE, wall sites get the normalised sum of their wall-link vectors as normal. */
+int hlbg_write_gmy(const hlbg_geometry *geom, const char *path);
 /* Access the generated geometry and its iolets (pointers stay owned by the handle). */
 int hlbg_synth_view(void *geom_handle, hlbg_geometry *out, int64_t *n_fluid_sites,
                     int32_t *n_inlets, int32_t *n_outlets);
