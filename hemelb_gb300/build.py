@@ -27,6 +27,7 @@ UNITS = [
     ("lb_fp64.cu", ["--fmad=false"]),
     ("lb_fp32.cu", []),
     ("capi.cu", ["--fmad=false"]),
+    ("nn_kernels.cu", []),
 ]
 HOST_UNITS = ["synthgeo.cpp"]
 
@@ -53,7 +54,8 @@ def build(force: bool = False, verbose: bool = False, defines=(), out: str | Non
     bdir = build_dir or BUILD
     os.makedirs(bdir, exist_ok=True)
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [
-        os.path.join(HERE, "..", "include", "hemelb_gb300.h")]
+        os.path.join(HERE, "..", "include", "hemelb_gb300.h"),
+        os.path.join(HERE, "..", "include", "hemelb_gb300_nn.h")]
     if not force and not _sources_newer(lib, deps + [__file__]):
         return lib
     jobs = []

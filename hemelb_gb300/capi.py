@@ -90,6 +90,7 @@ SIGNATURES = {
     "hlbg_collision_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
     "hlbg_device_bytes": (C.c_size_t, [C.c_void_p]),
     "hlbg_site_order": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "hlbg_site_coords": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "hlbg_init_equilibrium": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]),
     "hlbg_init_equilibrium_field": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "hlbg_step": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
@@ -113,6 +114,29 @@ SIGNATURES = {
     "hlbg_time_steps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "hlbg_time_kernels": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "hlbg_version": (C.c_char_p, []),
+    # include/hemelb_gb300_nn.h: the surrogate's kernels (device pointers, stream last)
+    "hlbg_nn_conv3d": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                 C.c_int32, C.c_void_p]),
+    "hlbg_nn_conv3d_wgrad": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                       C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "hlbg_nn_flip_transpose": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "hlbg_nn_relu_bwd": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "hlbg_nn_bias_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]),
+    "hlbg_nn_pool2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                C.c_int32, C.c_void_p]),
+    "hlbg_nn_up2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                              C.c_int32, C.c_void_p]),
+    "hlbg_nn_concat": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
+                                 C.c_void_p]),
+    "hlbg_nn_split": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int64,
+                                C.c_int32, C.c_void_p]),
+    "hlbg_nn_add": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "hlbg_nn_mse": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                              C.c_int32, C.c_float, C.c_void_p]),
+    "hlbg_nn_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                               C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, C.c_void_p]),
+    "hlbg_nn_to_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
 }
 
 _lib = None

@@ -703,6 +703,18 @@ int hlbg_site_order(const hlbg_ctx* ctx, int64_t* ref_to_slot) {
   return HLBG_OK;
 }
 
+int hlbg_site_coords(const hlbg_ctx* ctx, int32_t* xyz) {
+  if (!ctx || !xyz) return HLBG_ERR_INVAL;
+  for (int64_t i = 0; i < ctx->nsites; ++i) {
+    const int64_t s = ctx->h_ref2slot[i], b = s >> 9;
+    const int l = (int)(s & 511);
+    xyz[3 * i] = ctx->h_block_xyz[3 * b] * 8 + (l >> 6);
+    xyz[3 * i + 1] = ctx->h_block_xyz[3 * b + 1] * 8 + ((l >> 3) & 7);
+    xyz[3 * i + 2] = ctx->h_block_xyz[3 * b + 2] * 8 + (l & 7);
+  }
+  return HLBG_OK;
+}
+
 int hlbg_init_equilibrium(hlbg_ctx* ctx, double density, double vx, double vy, double vz) {
   if (!ctx) return HLBG_ERR_INVAL;
   if (!(density > 0.0)) return fail(ctx, HLBG_ERR_INVAL, "density must be positive");

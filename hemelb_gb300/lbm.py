@@ -246,6 +246,11 @@ class LBM:
         check(self._lib.hlbg_site_order(self._ctx, out.ctypes.data_as(C.POINTER(C.c_int64))), self._ctx)
         return out
 
+    def site_coords(self) -> np.ndarray:
+        out = np.empty((self.n_sites, 3), dtype=np.int32)
+        check(self._lib.hlbg_site_coords(self._ctx, out.ctypes.data_as(C.POINTER(C.c_int32))), self._ctx)
+        return out
+
     # ---- LBM::SetInitialConditions -------------------------------------------
     def SetInitialConditions(self, density=1.0, velocity=(0.0, 0.0, 0.0)):
         check(self._lib.hlbg_init_equilibrium(self._ctx, density, *velocity), self._ctx)

@@ -196,6 +196,9 @@ size_t hlbg_device_bytes(const hlbg_ctx *ctx);
  * collision type, then Morton block order, then in-block order). */
 int hlbg_site_order(const hlbg_ctx *ctx, int64_t *ref_to_slot);
 
+/* Global coordinates of the sites in contiguous order (xyz[N*3]; Domain::GetGlobalSiteCoords). */
+int hlbg_site_coords(const hlbg_ctx *ctx, int32_t *xyz);
+
 /* Uniform equilibrium initial condition (both f arrays), time step reset to 1. */
 int hlbg_init_equilibrium(hlbg_ctx *ctx, double density, double vx, double vy, double vz);
 /* Per-site equilibrium start from host fields in contiguous site order

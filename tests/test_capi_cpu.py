@@ -14,11 +14,11 @@ from oracle.oracle import OracleLBM
 from tests.helpers import CX19, CY19, CZ19
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADER = os.path.join(ROOT, "include", "hemelb_gb300.h")
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("hemelb_gb300.h", "hemelb_gb300_nn.h")]
 
 
 def declared_symbols():
-    text = open(HEADER).read()
+    text = "".join(open(h).read() for h in HEADERS)
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(hlbg_[a-z0-9_]+)\s*\(", text)))
 
