@@ -73,6 +73,8 @@ SIGNATURES = {
     "hlbg_synth_members": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.POINTER(C.c_int32)),
                                      C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.POINTER(C.c_double)),
                                      C.POINTER(C.POINTER(C.c_int64))]),
+    "hlbg_synth_vessel_box": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "hlbg_synth_distance": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     "hlbg_write_gmy": (C.c_int, [C.POINTER(Geometry), C.c_char_p]),
     "hlbg_read_gmy": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "hlbg_synth_view": (C.c_int, [C.c_void_p, C.POINTER(Geometry), C.POINTER(C.c_int64),
@@ -97,6 +99,9 @@ SIGNATURES = {
     "hlbg_sync": (C.c_int, [C.c_void_p]),
     "hlbg_step_graph": (C.c_int, [C.c_void_p, C.c_int32]),
     "hlbg_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "hlbg_run_to_steady": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int32,
+                                     C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "hlbg_average_time_levels": (C.c_int, [C.c_void_p]),
     "hlbg_set_block_tau": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_stream_and_collide_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "hlbg_post_step_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),

@@ -112,8 +112,10 @@ struct hlbg_ctx {
   double* d_blk_omega = nullptr;      // optional per-block (omega+, omega-)
   // CUDA graphs of k steps, keyed by (k, parity of the current array)
   struct GraphKey {
-    int n, cur;
-    bool operator<(const GraphKey& o) const { return n != o.n ? n < o.n : cur < o.cur; }
+    int n, cur, check;  // check: a steady-state check after every step
+    bool operator<(const GraphKey& o) const {
+      return n != o.n ? n < o.n : (cur != o.cur ? cur < o.cur : check < o.check);
+    }
   };
   std::map<GraphKey, cudaGraphExec_t> graphs;
   int32_t* d_io_rec = nullptr;    // records with at least one iolet link
@@ -140,6 +142,10 @@ struct hlbg_ctx {
   int64_t list_cap = 0;
   double* d_part = nullptr;  // monitor partials
   unsigned long long* d_part_bad = nullptr;
+  // steady-state detection: [threshold, last max |du|] and the SteadyArgs counters
+  double* d_steady = nullptr;
+  long long* d_steady_n = nullptr;
+  long long* h_steady_n = nullptr;  // pinned copy of the counters
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t dev_bytes = 0;
@@ -572,6 +578,90 @@ int run_post(hlbg_ctx* ctx, cudaStream_t st, const int32_t* slot, const int8_t* 
 
 }  // namespace
 
+namespace {
+
+// One replay of the graph of n steps (captured on first use per step count, array
+// parity and check flag), after refreshing the pinned iolet table for its steps.
+int graph_steps(hlbg_ctx* ctx, int n, bool check) {
+  if (ctx->n_io) {
+    CK(cudaEventSynchronize(ctx->io_copied));
+    for (int k = 0; k < n; ++k) {
+      uint64_t t1 = ctx->t1 + k;
+      double* row = ctx->h_io_tab + (size_t)k * 2 * ctx->n_io;
+      int j = 0;
+      for (auto* v : {&ctx->inlets, &ctx->outlets})
+        for (auto& io : *v) {
+          row[j] = iolet_density(ctx, io, t1 - 1);
+          row[ctx->n_io + j] = iolet_umax(io, (uint64_t)(unsigned int)t1);
+          ++j;
+        }
+    }
+  }
+  hlbg_ctx::GraphKey key{n, ctx->cur, check ? 1 : 0};
+  auto it = ctx->graphs.find(key);
+  if (it == ctx->graphs.end()) {
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = HLBG_OK;
+    if (ctx->n_io) {
+      cudaError_t e = cudaMemcpyAsync(ctx->d_io_tab, ctx->h_io_tab, sizeof(double) * 2 * ctx->n_io * n,
+                                      cudaMemcpyHostToDevice, ctx->stream);
+      if (e != cudaSuccess) rc = fail(ctx, HLBG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const int cur0 = ctx->cur;
+    const int64_t nparts = (ctx->nslot + 255) / 256;
+    StepArgs a;
+    for (int k = 0; k < n && !rc; ++k) {
+      fill_args(ctx, a);
+      a.iolet_rho = ctx->d_io_tab + (size_t)k * 2 * ctx->n_io;
+      a.iolet_umax = a.iolet_rho + ctx->n_io;
+      rc = launch_collide(ctx, a, ctx->stream);
+      if (!rc) rc = run_post(ctx, ctx->stream, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps);
+      ctx->cur ^= 1;
+      if (!rc && check) {
+        MonitorArgs ma{};
+        ma.f_cur = ctx->f[ctx->cur];
+        ma.f_prev = ctx->f[ctx->cur ^ 1];
+        ma.stride = ctx->nslot;
+        ma.nslot = ctx->nslot;
+        ma.site_code = ctx->d_site_code;
+        ma.block_bulk = ctx->d_block_bulk;
+        ma.part_mass = ctx->d_part;
+        ma.part_max = ctx->d_part + nparts;
+        ma.part_min = ctx->d_part + 2 * nparts;
+        ma.part_bad = ctx->d_part_bad;
+        ma.fp16_scale = ctx->fp16_scale;
+        ma.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+        SteadyArgs sa{ctx->d_steady, ctx->d_steady + 1, ctx->d_steady_n};
+        switch (ctx->prec) {
+          case 0: launch_steady_check_0(ma, sa, ctx->stream); break;
+          case 1: launch_steady_check_1(ma, sa, ctx->stream); break;
+          default: launch_steady_check_2(ma, sa, ctx->stream); break;
+        }
+      }
+    }
+    ctx->cur = cur0;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+    it = ctx->graphs.emplace(key, exec).first;
+  }
+  CK(cudaGraphLaunch(it->second, ctx->stream));
+  if (ctx->n_io) CK(cudaEventRecord(ctx->io_copied, ctx->stream));
+  ctx->cur ^= (n & 1);
+  ctx->t1 += n;
+  return HLBG_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* hlbg_version(void) { return "hemelb_gb300 0.1 (sm_103a, D3Q19)"; }
@@ -586,12 +676,14 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_rec_slot,  ctx->d_io_rec,
                   ctx->d_ps_slot,   ctx->d_ps_dir,    ctx->d_ps_q,      ctx->d_iolets,
                   ctx->d_io_tab,    ctx->d_stage,     ctx->d_stage_rho, ctx->d_stage_u,
-                  ctx->d_list,      ctx->d_part,      ctx->d_part_bad};
+                  ctx->d_list,      ctx->d_part,      ctx->d_part_bad,  ctx->d_steady,
+                  ctx->d_steady_n};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
   if (ctx->d_blk_omega) cudaFree(ctx->d_blk_omega);
   if (ctx->h_io_tab) cudaFreeHost(ctx->h_io_tab);
+  if (ctx->h_steady_n) cudaFreeHost(ctx->h_steady_n);
   if (ctx->io_copied) cudaEventDestroy(ctx->io_copied);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -832,67 +924,93 @@ int hlbg_set_block_tau(hlbg_ctx* ctx, const double* tau) {
 }
 
 int hlbg_step_graph(hlbg_ctx* ctx, int32_t nsteps) {
-  // nsteps time steps as one CUDA graph launch: the iolet-table copy and every
+  // nsteps time steps as CUDA graph launches: the iolet-table copy and every
   // kernel of every step, captured once per (step count, array parity) and
   // replayed.  The host refreshes the pinned iolet table before each replay.
   if (!ctx || nsteps < 0) return HLBG_ERR_INVAL;
   if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
   for (int done = 0; done < nsteps;) {
     const int n = std::min(kStepBatch, nsteps - done);
-    if (ctx->n_io) {
-      CK(cudaEventSynchronize(ctx->io_copied));
-      for (int k = 0; k < n; ++k) {
-        uint64_t t1 = ctx->t1 + k;
-        double* row = ctx->h_io_tab + (size_t)k * 2 * ctx->n_io;
-        int j = 0;
-        for (auto* v : {&ctx->inlets, &ctx->outlets})
-          for (auto& io : *v) {
-            row[j] = iolet_density(ctx, io, t1 - 1);
-            row[ctx->n_io + j] = iolet_umax(io, (uint64_t)(unsigned int)t1);
-            ++j;
-          }
-      }
-    }
-    hlbg_ctx::GraphKey key{n, ctx->cur};
-    auto it = ctx->graphs.find(key);
-    if (it == ctx->graphs.end()) {
-      cudaGraph_t graph = nullptr;
-      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      int rc = HLBG_OK;
-      if (ctx->n_io) {
-        cudaError_t e = cudaMemcpyAsync(ctx->d_io_tab, ctx->h_io_tab, sizeof(double) * 2 * ctx->n_io * n,
-                                        cudaMemcpyHostToDevice, ctx->stream);
-        if (e != cudaSuccess) rc = fail(ctx, HLBG_ERR_CUDA, cudaGetErrorString(e));
-      }
-      const int cur0 = ctx->cur;
-      StepArgs a;
-      for (int k = 0; k < n && !rc; ++k) {
-        fill_args(ctx, a);
-        a.iolet_rho = ctx->d_io_tab + (size_t)k * 2 * ctx->n_io;
-        a.iolet_umax = a.iolet_rho + ctx->n_io;
-        rc = launch_collide(ctx, a, ctx->stream);
-        if (!rc) rc = run_post(ctx, ctx->stream, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps);
-        ctx->cur ^= 1;
-      }
-      ctx->cur = cur0;
-      cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
-      if (rc) {
-        if (graph) cudaGraphDestroy(graph);
-        return rc;
-      }
-      if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-      cudaGraphExec_t exec = nullptr;
-      e = cudaGraphInstantiate(&exec, graph, 0);
-      cudaGraphDestroy(graph);
-      if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
-      it = ctx->graphs.emplace(key, exec).first;
-    }
-    CK(cudaGraphLaunch(it->second, ctx->stream));
-    if (ctx->n_io) CK(cudaEventRecord(ctx->io_copied, ctx->stream));
-    ctx->cur ^= (n & 1);
-    ctx->t1 += n;
+    int rc = graph_steps(ctx, n, false);
+    if (rc) return rc;
     done += n;
   }
+  return HLBG_OK;
+}
+
+int hlbg_run_to_steady(hlbg_ctx* ctx, double tol, double u_ref, int64_t max_steps, int32_t check_batch,
+                       int64_t* steps_to_steady, int64_t* steps_run, double* final_rel_du) {
+  // Time steps until StabilityTester's convergence test holds: after every step,
+  // max over sites |u_new - u_old| / U_ref <= tol (Code/lb/StabilityTester.h:91-183),
+  // evaluated on the device.  Steps run in CUDA graphs of check_batch steps, each
+  // step followed by its check; the host reads the device counters after each
+  // batch, so up to check_batch - 1 steps run past the first converged one.
+  if (!ctx || !(tol > 0.0) || !(u_ref > 0.0) || max_steps < 1 || check_batch < 1 ||
+      check_batch > kStepBatch)
+    return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  const int64_t nparts = (ctx->nslot + 255) / 256;
+  if (!ctx->d_part) {
+    int rc = dev_alloc(ctx, &ctx->d_part, (size_t)nparts * 3);
+    if (!rc) rc = dev_alloc(ctx, &ctx->d_part_bad, (size_t)nparts);
+    if (rc) return rc;
+  }
+  if (!ctx->d_steady) {
+    int rc = dev_alloc(ctx, &ctx->d_steady, 2);
+    if (!rc) rc = dev_alloc(ctx, &ctx->d_steady_n, 3);
+    if (rc) return rc;
+    CK(cudaMallocHost((void**)&ctx->h_steady_n, 3 * sizeof(long long)));
+  }
+  const double hv[2] = {tol * u_ref, -1.0};
+  const long long hn[3] = {0, -1, -1};
+  CK(cudaMemcpyAsync(ctx->d_steady, hv, sizeof(hv), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_steady_n, hn, sizeof(hn), cudaMemcpyHostToDevice, ctx->stream));
+  int64_t run = 0;
+  int status = HLBG_ERR_TIMEOUT;
+  while (run < max_steps) {
+    const int n = (int)std::min<int64_t>(check_batch, max_steps - run);
+    int rc = graph_steps(ctx, n, true);
+    if (rc) return rc;
+    run += n;
+    CK(cudaMemcpyAsync(ctx->h_steady_n, ctx->d_steady_n, 3 * sizeof(long long), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_steady_n[2] >= 0) {
+      status = HLBG_ERR_UNSTABLE;
+      break;
+    }
+    if (ctx->h_steady_n[1] >= 0) {
+      status = HLBG_OK;
+      break;
+    }
+  }
+  double last = 0.0;
+  CK(cudaMemcpy(&last, ctx->d_steady + 1, sizeof(double), cudaMemcpyDeviceToHost));
+  if (steps_to_steady) *steps_to_steady = status == HLBG_OK ? ctx->h_steady_n[1] : -1;
+  if (steps_run) *steps_run = run;
+  if (final_rel_du) *final_rel_du = last / u_ref;
+  if (status == HLBG_ERR_UNSTABLE) return fail(ctx, status, "unstable: a distribution is not positive");
+  if (status == HLBG_ERR_TIMEOUT) return fail(ctx, status, "not converged within max_steps");
+  return HLBG_OK;
+}
+
+int hlbg_average_time_levels(hlbg_ctx* ctx) {
+  if (!ctx) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  AverageArgs aa{};
+  aa.f_cur = ctx->f[ctx->cur];
+  aa.f_prev = ctx->f[ctx->cur ^ 1];
+  aa.nslot = ctx->nslot;
+  aa.site_code = ctx->d_site_code;
+  aa.block_bulk = ctx->d_block_bulk;
+  aa.fp16_scale = ctx->fp16_scale;
+  aa.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+  switch (ctx->prec) {
+    case 0: launch_average_0(aa, ctx->stream); break;
+    case 1: launch_average_1(aa, ctx->stream); break;
+    default: launch_average_2(aa, ctx->stream); break;
+  }
+  CK(cudaGetLastError());
   return HLBG_OK;
 }
 

@@ -674,6 +674,47 @@ static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, in
   }
 }
 
+// Final reduction of the monitor partials for steady-state detection: one check
+// per call, counted on the device so that a captured graph of many steps (each
+// followed by its check) records the first converged step without host reads.
+static __global__ void __launch_bounds__(256) k_steady_final(MonitorArgs ma, int64_t nparts, SteadyArgs sa) {
+  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  for (int64_t i = threadIdx.x; i < nparts; i += blockDim.x)
+    mon_combine(acc, MonAcc{ma.part_mass[i], ma.part_max[i], ma.part_min[i], ma.part_bad[i]});
+  __syncthreads();
+  acc = mon_block(acc);
+  if (threadIdx.x == 0) {
+    const long long n = sa.counters[0] + 1;
+    sa.counters[0] = n;
+    *sa.last_du = acc.maxdu;
+    if (acc.bad && sa.counters[2] < 0) sa.counters[2] = n;
+    // a NaN maximum compares false and never counts as converged
+    if (acc.maxdu <= *sa.threshold && sa.counters[1] < 0) sa.counters[1] = n;
+  }
+}
+
+// Mean of the two time levels on every fluid slot (the arrays hold consecutive
+// states right after a step): removes the period-two component of the state.
+template <int P>
+__global__ void __launch_bounds__(256) k_average(AverageArgs aa) {
+  using St = Store<P>;
+  using S = typename St::S;
+  StepArgs a{};
+  a.fp16_scale = aa.fp16_scale;
+  a.fp16_inv_scale = aa.fp16_inv_scale;
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t code = (s < aa.nslot) ? (aa.block_bulk[s >> 9] ? 1u : aa.site_code[s]) : 0u;
+  if (code == 0) return;
+  const int64_t off = fidx(s, 0);
+  S* fc = static_cast<S*>(aa.f_cur) + off;
+  const S* fp = static_cast<const S*>(aa.f_prev) + off;
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    const auto v = St::load(fc, d * kSites, a) + St::load(fp, d * kSites, a);
+    St::store(fc, d * kSites, v * 0.5f, a);
+  }
+}
+
 }  // namespace hlbg
 
 namespace hlbg {
@@ -748,5 +789,14 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     const int64_t nparts = (ma.nslot + 255) / 256;                                              \
     k_monitor<P><<<(unsigned)nparts, 256, 0, st>>>(ma);                                         \
     k_monitor_final<<<1, 256, 0, st>>>(ma, nparts);                                             \
+  }                                                                                             \
+  void launch_steady_check_##P(const MonitorArgs& ma, const SteadyArgs& sa, cudaStream_t st) {  \
+    const int64_t nparts = (ma.nslot + 255) / 256;                                              \
+    k_monitor<P><<<(unsigned)nparts, 256, 0, st>>>(ma);                                         \
+    k_steady_final<<<1, 256, 0, st>>>(ma, nparts, sa);                                          \
+  }                                                                                             \
+  void launch_average_##P(const AverageArgs& aa, cudaStream_t st) {                             \
+    unsigned g = (unsigned)((aa.nslot + 255) / 256);                                            \
+    if (g) k_average<P><<<g, 256, 0, st>>>(aa);                                                 \
   }                                                                                             \
   }

@@ -70,6 +70,26 @@ struct MonitorArgs {
   float fp16_scale, fp16_inv_scale;
 };
 
+// Steady-state detection after every step (StabilityTester with its convergence
+// check, Code/lb/StabilityTester.h:91-183): the final reduction of the monitor
+// partials counts checks and records the first check whose max |u_new - u_old|
+// is within the threshold (tol * U_ref), and the first unstable one.
+struct SteadyArgs {
+  const double* threshold;  // tol * U_ref
+  double* last_du;          // max |du| of the latest check
+  long long* counters;      // [checks done, first converged check or -1, first unstable check or -1]
+};
+
+// f_cur <- (f_cur + f_prev) / 2 on every fluid slot
+struct AverageArgs {
+  void* f_cur;
+  const void* f_prev;
+  int64_t nslot;
+  const uint32_t* site_code;
+  const uint8_t* block_bulk;
+  float fp16_scale, fp16_inv_scale;
+};
+
 #define HLBG_DECLARE(P)                                                              \
   void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st,  \
                                  int variant);                                           \
@@ -81,7 +101,9 @@ struct MonitorArgs {
   void launch_gather_##P(const GatherArgs& ga, cudaStream_t st);                     \
   void launch_scatter_##P(const GatherArgs& ga, cudaStream_t st);                    \
   void launch_macro_##P(const GatherArgs& ga, cudaStream_t st);                      \
-  void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st);
+  void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st);          \
+  void launch_steady_check_##P(const MonitorArgs& ma, const SteadyArgs& sa, cudaStream_t st); \
+  void launch_average_##P(const AverageArgs& aa, cudaStream_t st);
 
 HLBG_DECLARE(0)
 HLBG_DECLARE(1)

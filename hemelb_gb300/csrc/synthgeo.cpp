@@ -1075,4 +1075,106 @@ int hlbg_synth_iolet(void* handle, int32_t is_outlet, int32_t index, double posi
 
 void hlbg_synth_free(void* handle) { delete static_cast<Geometry*>(handle); }
 
+// One seeded vessel in a fixed cubic box of box_sites^3 voxels (a multiple of 8);
+// lengths below are for a 96 box and scale with box_sites / 96:
+// kind 0 a stenosed pipe along z (radius U[6,14], Gaussian narrowing of depth
+// U[0,0.6] and width U[0.5,1.5] x radius, centre z in U[0.35,0.65] x box, axis
+// offset up to 10 sites from the box centre); kind 1 a bifurcation (parent radius
+// U[6,12] along z up to a split at U[0.3,0.5] x box, Murray daughters with split
+// ratio U[0.3,0.7], half-angles U[20,45] degrees in a random plane, each running
+// to the box margin).  Inlet plane z = 1.5 (normal +z), outlets at the far ends.
+// Simple bounce-back geometry (no cut distances).
+int hlbg_synth_vessel_box(uint64_t seed, int32_t box_sites, int32_t kind, int32_t q, void** handle) {
+  if (!handle || box_sites < 32 || box_sites % kBlock || (kind != 0 && kind != 1) || (q != 15 && q != 19))
+    return HLBG_ERR_INVAL;
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  const double B = box_sites;
+  const double sc = B / 96.0;
+  auto* g = new Geometry();
+  g->q = q;
+  g->with_cuts = false;
+  const double z_in = 1.5;
+  const Vec axis0{0.5 * B - 0.5 + (U(rng) - 0.5) * 20.0 * sc, 0.5 * B - 0.5 + (U(rng) - 0.5) * 20.0 * sc, 0.0};
+  if (kind == 0) {
+    const double r = (6.0 + 8.0 * U(rng)) * sc;
+    Shape s{};
+    s.kind = 1;
+    s.a = {axis0.x, axis0.y, z_in - 1.0};
+    s.b = {axis0.x, axis0.y, B - 1.5};
+    s.r = r;
+    s.depth = 0.6 * U(rng);
+    s.zc = (0.35 + 0.3 * U(rng)) * B;
+    s.sigma = (0.5 + U(rng)) * r;
+    g->shapes.push_back(s);
+    g->inlets.push_back(mk_iolet(0, 0, {axis0.x, axis0.y, z_in}, {0, 0, 1}, r));
+    g->outlets.push_back(mk_iolet(1, 0, {axis0.x, axis0.y, B - 2.5}, {0, 0, -1}, r));
+  } else {
+    const double r0 = (6.0 + 6.0 * U(rng)) * sc;
+    const double zs = (0.3 + 0.2 * U(rng)) * B;
+    const double split = 0.3 + 0.4 * U(rng);
+    const double th1 = (20.0 + 25.0 * U(rng)) * M_PI / 180.0, th2 = (20.0 + 25.0 * U(rng)) * M_PI / 180.0;
+    const double phi = 2.0 * M_PI * U(rng);
+    const double r1 = r0 * std::cbrt(split), r2 = r0 * std::cbrt(1.0 - split);
+    const Vec a{axis0.x, axis0.y, z_in - 1.0}, b{axis0.x, axis0.y, zs};
+    g->shapes.push_back(cyl(a, b, r0, false, true));
+    g->inlets.push_back(mk_iolet(0, 0, {axis0.x, axis0.y, z_in}, {0, 0, 1}, r0));
+    const Vec zdir{0, 0, 1};
+    const Vec dirs[2] = {deflect(zdir, th1, phi), deflect(zdir, th2, phi + M_PI)};
+    const double rs[2] = {r1, r2};
+    for (int k = 0; k < 2; ++k) {
+      // run to the margin: lateral faces r + 3 sites in, top face 2.5 sites in
+      const Vec d = dirs[k];
+      const double m = rs[k] + 3.0 * sc;
+      double len = 1e30;
+      const double lo[3] = {m, m, 0.0}, hi[3] = {B - 1.0 - m, B - 1.0 - m, B - 2.5};
+      const double p0[3] = {b.x, b.y, b.z}, dv[3] = {d.x, d.y, d.z};
+      for (int ax = 0; ax < 3; ++ax) {
+        if (dv[ax] > 1e-9) len = std::min(len, (hi[ax] - p0[ax]) / dv[ax]);
+        if (dv[ax] < -1e-9) len = std::min(len, (lo[ax] - p0[ax]) / dv[ax]);
+      }
+      len = std::max(len, 2.0 * rs[k]);
+      const Vec e = add(b, mul(d, len));
+      g->shapes.push_back(cyl(b, e, rs[k], true, false));
+      g->outlets.push_back(mk_iolet(1, k, e, mul(d, -1.0), rs[k]));
+    }
+  }
+  place(*g, box_sites);
+  return finish(g, 0, handle);
+}
+
+// Signed distance to the vessel wall at every voxel centre of the box (positive
+// inside): for each shape its radius (local radius for the stenosed pipe) minus
+// the distance to its axis segment, the largest over shapes.  out holds
+// box^3 floats, x slowest and z fastest.
+int hlbg_synth_distance(void* handle, float* out) {
+  if (!handle || !out) return HLBG_ERR_INVAL;
+  auto* g = static_cast<Geometry*>(handle);
+  const int X = g->nb[0] * kBlock, Y = g->nb[1] * kBlock, Z = g->nb[2] * kBlock;
+  for (int x = 0; x < X; ++x)
+    for (int y = 0; y < Y; ++y)
+      for (int z = 0; z < Z; ++z) {
+        const Vec p{(double)x, (double)y, (double)z};
+        double best = -1e30;
+        for (const Shape& s : g->shapes) {
+          double sd;
+          if (s.kind == 0) {
+            const Vec v = sub(s.b, s.a), w = sub(p, s.a);
+            double t = dot(w, v) / dot(v, v);
+            t = std::min(1.0, std::max(0.0, t));
+            const Vec c = sub(w, mul(v, t));
+            sd = s.r - std::sqrt(dot(c, c));
+          } else {
+            const double dz = p.z - s.zc;
+            const double rr = s.r * (1.0 - s.depth * std::exp(-dz * dz / (2.0 * s.sigma * s.sigma)));
+            const double dx = p.x - s.a.x, dy = p.y - s.a.y;
+            sd = rr - std::sqrt(dx * dx + dy * dy);
+          }
+          best = std::max(best, sd);
+        }
+        out[((size_t)x * Y + y) * Z + z] = (float)best;
+      }
+  return HLBG_OK;
+}
+
 }  // extern "C"

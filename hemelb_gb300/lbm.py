@@ -133,6 +133,37 @@ class SyntheticGeometry:
                 _np(shape, 3 * m, np.float64).reshape(m, 3).copy(), _np(sites, m, np.int64).copy())
 
     @classmethod
+    def vessel_box(cls, seed: int, box_sites: int = 96, kind: int = 0, q: int = 19):
+        """Seeded stenosis (kind 0) or bifurcation (kind 1) in a fixed box."""
+        lib = capi.load()
+        h = C.c_void_p()
+        check(lib.hlbg_synth_vessel_box(seed, box_sites, kind, q, C.byref(h)))
+        return cls(h, lib)
+
+    def box_shape(self):
+        return tuple(int(b) * 8 for b in self.view.blocks)
+
+    def signed_distance(self) -> np.ndarray:
+        """Signed distance to the wall on the box grid, shape (X, Y, Z), positive inside."""
+        out = np.empty(self.box_shape(), dtype=np.float32)
+        check(self._lib.hlbg_synth_distance(self._h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def fluid_grid(self) -> np.ndarray:
+        """Fluid flags on the box grid, shape (X, Y, Z), from the block bitmaps."""
+        X, Y, Z = self.box_shape()
+        grid = np.zeros((X, Y, Z), dtype=bool)
+        bc = self.block_coords.reshape(-1, 3)
+        bits = np.unpackbits(self.fluid_mask.reshape(-1, 8).view(np.uint8), axis=1,
+                             bitorder="little").astype(bool)  # [blocks, 512], local (x*8+y)*8+z
+        loc = np.arange(512)
+        lx, ly, lz = loc >> 6, (loc >> 3) & 7, loc & 7
+        for b in range(bc.shape[0]):
+            m = bits[b]
+            grid[bc[b, 0] * 8 + lx[m], bc[b, 1] * 8 + ly[m], bc[b, 2] * 8 + lz[m]] = True
+        return grid
+
+    @classmethod
     def tree(cls, seed=7, box_sites=1280, n_roots=1, depth=7, root_radius=60.0, q=19,
              with_cuts=False, n_threads=0):
         lib = capi.load()
@@ -271,6 +302,22 @@ class LBM:
         check(self._lib.hlbg_step_graph(self._ctx, n), self._ctx)
         if sync:
             check(self._lib.hlbg_sync(self._ctx), self._ctx)
+
+    def RunToSteady(self, tol: float, u_ref: float, max_steps: int = 1_000_000,
+                    check_batch: int = 25):
+        """Step until max |u_new - u_old| / u_ref <= tol (checked after every step on
+        the device).  Returns (steps_to_steady, steps_run, final_rel_du, status);
+        status is 0 when converged, HLBG_ERR_TIMEOUT or HLBG_ERR_UNSTABLE otherwise."""
+        a, b, d = C.c_int64(), C.c_int64(), C.c_double()
+        rc = self._lib.hlbg_run_to_steady(self._ctx, tol, u_ref, max_steps, check_batch,
+                                          C.byref(a), C.byref(b), C.byref(d))
+        if rc not in (capi.HLBG_OK, capi.HLBG_ERR_TIMEOUT, capi.HLBG_ERR_UNSTABLE):
+            check(rc, self._ctx)
+        return a.value, b.value, d.value, rc
+
+    def AverageTimeLevels(self):
+        """Current distributions <- mean of the two time levels (right after a step)."""
+        check(self._lib.hlbg_average_time_levels(self._ctx), self._ctx)
 
     def autotune(self, steps_per_trial: int = 5):
         v = C.c_int32()

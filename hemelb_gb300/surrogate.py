@@ -1,0 +1,491 @@
+"""Learned warm start for steady vessel flow.
+
+A 3-D convolutional U-Net predicts the steady velocity and pressure of a vessel
+from its geometry (fluid mask, signed distance to the wall, inlet pressure and
+relaxation time on a cubic voxel box).  The solver then starts from the
+equilibrium on that prediction (``hlbg_init_equilibrium_field``, the
+reference's EquilibriumInitialCondition applied per site,
+Code/lb/InitialCondition.hpp:40-52), instead of from rest, and steps until the
+StabilityTester convergence test holds (``hlbg_run_to_steady``).
+
+The network is trained and run on the GPU by the library's own BF16 tensor-core
+kernels (include/hemelb_gb300_nn.h: implicit-GEMM 3-D convolutions and their
+input and weight gradients, pooling, upsampling, masked MSE, Adam); torch only
+provides device memory and the stream.  Activations and weights are BF16, every
+product accumulates in FP32, and the master weights and the network output are
+FP32.
+
+Targets come from the plain FP64 D3Q19 LBGK solver itself: bounce-back walls,
+Nash pressure iolets (inlet density 1 + drho, outlets 1), run from rest to
+max |du| / U_ref <= 1e-6.  Training samples are solved with a one-off average of
+the first two time levels (``hlbg_average_time_levels``), which removes the
+lattice's slowly decaying staggered-momentum mode and shortens data generation
+about sixfold; held-out samples are solved exactly as the reference would, from
+rest, and that plain solve judges the error of every warm-started run.
+
+U_ref, the StabilityTester reference speed, is the Poiseuille centreline speed
+of the inlet tube under the mean pressure gradient: (drho c_s^2 / box) R_in^2 / (4 nu).
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import capi, nn
+from .lbm import Case, InOutLetCosine, LbmParameters, SyntheticGeometry
+
+CS2 = 1.0 / 3.0
+N_IN = 16   # input channels (7 used, the rest zero: the convolution wants multiples of 16)
+N_OUT = 16  # output channels (u_x, u_y, u_z, p used; the rest are trained towards zero)
+
+
+# ---------------------------------------------------------------------------
+# samples and the plain solver
+# ---------------------------------------------------------------------------
+@dataclass
+class Sample:
+    """One seeded vessel in a box with its flow parameters."""
+
+    seed: int
+    kind: int      # 0 stenosis, 1 bifurcation
+    tau: float     # U[0.7, 1.0]
+    drho: float    # inlet density excess, U[5e-4, 3e-3]
+    box: int = 96
+
+    @staticmethod
+    def draw(index: int, base_seed: int = 20240607, box: int = 96) -> "Sample":
+        rng = np.random.default_rng([base_seed, index])
+        return Sample(seed=int(rng.integers(1 << 62)), kind=int(rng.integers(2)),
+                      tau=float(rng.uniform(0.7, 1.0)), drho=float(rng.uniform(5e-4, 3e-3)),
+                      box=box)
+
+    def geometry(self) -> SyntheticGeometry:
+        return SyntheticGeometry.vessel_box(self.seed, self.box, self.kind, 19)
+
+    def case(self, g: SyntheticGeometry | None = None) -> Case:
+        g = g or self.geometry()
+        inl, outl = [], []
+        for k in range(g.n_inlets):
+            pos, nrm, _ = g.iolet(False, k)
+            inl.append(InOutLetCosine(pos, nrm, density_mean=1.0 + self.drho))
+        for k in range(g.n_outlets):
+            pos, nrm, _ = g.iolet(True, k)
+            outl.append(InOutLetCosine(pos, nrm, density_mean=1.0))
+        p = LbmParameters(tau=self.tau, kernel=capi.KERNEL_LBGK, wall=capi.WALL_SBB,
+                          inlet=capi.IOLET_NASH, outlet=capi.IOLET_NASH, precision=capi.FP64)
+        return Case("vessel_box_%d" % self.seed, g, p, inl, outl, 0)
+
+    def u_ref(self, g: SyntheticGeometry) -> float:
+        r_in = g.iolet(False, 0)[2]
+        nu = (self.tau - 0.5) * CS2
+        return (self.drho * CS2 / self.box) * r_in * r_in / (4.0 * nu)
+
+
+class SteadyRunner:
+    """One solver context for a sample, reused by every start.  Its CUDA graphs (one
+    per array parity) are captured before any timed run, so a timed run covers the
+    initial condition, the optional averaging step and the steps to steady state."""
+
+    def __init__(self, case: Case, u_ref: float, tol: float = 1e-6, check_batch: int = 25):
+        self.s = case.solver()
+        self.u_ref, self.tol, self.check_batch = u_ref, tol, check_batch
+        self.coords = self.s.site_coords()
+        for pre in (0, 1):  # capture the graphs of both parities, untimed
+            self.s.SetInitialConditions()
+            if pre:
+                self.s.DoTimeStep(1)
+            self.s.RunToSteady(tol, u_ref, check_batch, check_batch)
+
+    def run(self, start=None, average: bool = False, max_steps: int = 400_000):
+        """From rest (start None) or from the equilibrium on start(coords) -> (rho, u)
+        in contiguous site order.  Returns (record, rho, u) of the final state."""
+        s = self.s
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if start is None:
+            s.SetInitialConditions()
+        else:
+            rho0, u0 = start(self.coords)
+            s.SetInitialField(rho0, u0)
+        t_init = time.perf_counter() - t0
+        pre = 0
+        if average:
+            s.DoTimeStep(1, sync=False)
+            s.AverageTimeLevels()
+            pre = 1
+        steps, run, du, rc = s.RunToSteady(self.tol, self.u_ref, max_steps, self.check_batch)
+        seconds = time.perf_counter() - t0
+        rec = {"steps": steps + pre if rc == 0 else -1, "steps_run": run + pre, "seconds": seconds,
+               "init_seconds": t_init, "final_rel_du": du, "status": rc}
+        rho, u = s.macro()
+        return rec, rho, u
+
+    def close(self):
+        self.s.close()
+
+
+# ---------------------------------------------------------------------------
+# network inputs and targets on the box grid
+# ---------------------------------------------------------------------------
+class Grids:
+    """Compact per-sample grids on the device: fluid mask (uint8), signed distance
+    (FP16), scalar parameters, and normalised targets (FP32 u/U_ref, (rho-1)/drho)."""
+
+    def __init__(self, n: int, box: int, device="cuda", with_targets=True):
+        shp = (n, box, box, box)
+        self.box = box
+        self.mask = torch.zeros(shp, dtype=torch.uint8, device=device)
+        self.sdf = torch.zeros(shp, dtype=torch.float16, device=device)
+        self.scal = torch.zeros((n, 2), dtype=torch.float32, device=device)
+        self.target = torch.zeros(shp + (4,), dtype=torch.float32, device=device) if with_targets else None
+        c = (torch.arange(box, dtype=torch.float32, device=device) + 0.5) / box - 0.5
+        self.coord = torch.stack(torch.meshgrid(c, c, c, indexing="ij"), dim=-1)  # (B, B, B, 3)
+
+    def put(self, i: int, g: SyntheticGeometry, smp: Sample, coords=None, rho=None, u=None, u_ref=None):
+        fl = g.fluid_grid()
+        self.mask[i] = torch.from_numpy(fl.astype(np.uint8)).to(self.mask.device)
+        sd = np.clip(g.signed_distance() / 8.0, -2.0, 2.0)
+        self.sdf[i] = torch.from_numpy(sd.astype(np.float16)).to(self.sdf.device)
+        self.scal[i, 0] = (smp.drho - 1.75e-3) / 1.25e-3
+        self.scal[i, 1] = (smp.tau - 0.85) / 0.15
+        if coords is not None and self.target is not None:
+            t = np.zeros((self.box,) * 3 + (4,), dtype=np.float32)
+            x, y, z = coords[:, 0], coords[:, 1], coords[:, 2]
+            t[x, y, z, 0:3] = u / u_ref
+            t[x, y, z, 3] = (rho - 1.0) / smp.drho
+            self.target[i] = torch.from_numpy(t).to(self.target.device)
+
+    def features(self, idx) -> torch.Tensor:
+        """BF16 input tensor (n, B, B, B, 16) for the samples idx."""
+        idx = torch.as_tensor(idx, device=self.mask.device)
+        n = idx.numel()
+        f = torch.zeros((n,) + (self.box,) * 3 + (N_IN,), dtype=torch.float32, device=self.mask.device)
+        f[..., 0] = self.mask[idx].float()
+        f[..., 1] = self.sdf[idx].float()
+        f[..., 2] = self.scal[idx, 0].view(n, 1, 1, 1)
+        f[..., 3] = self.scal[idx, 1].view(n, 1, 1, 1)
+        f[..., 4:7] = self.coord
+        return f.to(torch.bfloat16).contiguous()
+
+    def targets(self, idx):
+        """(FP32 targets padded to 16 channels, FP32 fluid mask) for the samples idx."""
+        idx = torch.as_tensor(idx, device=self.mask.device)
+        t = torch.zeros(self.target[idx].shape[:-1] + (N_OUT,), dtype=torch.float32,
+                        device=self.mask.device)
+        t[..., :4] = self.target[idx]
+        return t.contiguous(), self.mask[idx].float().contiguous()
+
+
+# ---------------------------------------------------------------------------
+# the U-Net, forward and backward by hand on the library's kernels
+# ---------------------------------------------------------------------------
+class Conv:
+    """3x3x3 (or 1x1x1) convolution, bias and optional ReLU, with FP32 master
+    weights, their BF16 copy, FP32 gradients and Adam moments."""
+
+    def __init__(self, cin, cout, rng, taps=27, relu=True, device="cuda", scale=1.0):
+        self.cin, self.cout, self.taps, self.relu = cin, cout, taps, relu
+        w = rng.standard_normal((taps, cout, cin)) * math.sqrt(2.0 / (taps * cin)) * scale
+        self.w = torch.tensor(w, dtype=torch.float32, device=device)
+        self.wb = self.w.to(torch.bfloat16)
+        self.b = torch.zeros(cout, dtype=torch.float32, device=device)
+        self.gw = torch.zeros_like(self.w)
+        self.gb = torch.zeros_like(self.b)
+        self.mw, self.vw = torch.zeros_like(self.w), torch.zeros_like(self.w)
+        self.mb, self.vb = torch.zeros_like(self.b), torch.zeros_like(self.b)
+        self.wt = torch.empty((taps, cout, cin), dtype=torch.bfloat16, device=device).transpose(1, 2).contiguous()
+        self.x = self.y = None
+
+    def n_params(self):
+        return self.w.numel() + self.b.numel()
+
+    def forward(self, x, out_f32=False):
+        shp = tuple(x.shape[:4]) + (self.cout,)
+        y = torch.empty(shp, dtype=torch.bfloat16, device=x.device)
+        y32 = torch.empty(shp, dtype=torch.float32, device=x.device) if out_f32 else None
+        nn.conv3d(x, self.wb, self.b, y, y32, taps=self.taps, relu=self.relu)
+        self.x, self.y = x, y
+        return y32 if out_f32 else y
+
+    def backward(self, dy, need_dx=True):
+        if self.relu:
+            nn.relu_backward(dy, self.y)
+        nn.bias_grad(dy, self.gb)
+        nn.conv3d_weight_grad(self.x, dy, self.gw)
+        dx = None
+        if need_dx:
+            dx = torch.empty(self.x.shape, dtype=torch.bfloat16, device=dy.device)
+            nn.conv3d_data_grad(dy, self.wb, dx, wt=self.wt)
+        self.x = self.y = None
+        return dx
+
+    def zero_grad(self):
+        self.gw.zero_()
+        self.gb.zero_()
+
+    def step(self, lr, t):
+        nn.adam(self.w, self.wb, self.gw, self.mw, self.vw, lr, t)
+        nn.adam(self.b, None, self.gb, self.mb, self.vb, lr, t)
+
+    def state(self):
+        return {"w": self.w.cpu().numpy(), "b": self.b.cpu().numpy()}
+
+    def load(self, st):
+        self.w.copy_(torch.from_numpy(st["w"]))
+        self.b.copy_(torch.from_numpy(st["b"]))
+        self.wb.copy_(self.w.to(torch.bfloat16))
+
+
+class UNet:
+    """Four-level 3-D U-Net: two 3x3x3 convolutions + ReLU per level, 2x average
+    pooling down, nearest 2x upsampling and skip concatenation up, a 1x1x1 FP32
+    head.  Channels (16, 48, 96, 192) give about 3.2M parameters."""
+
+    NAMES = ("e0a", "e0b", "e1a", "e1b", "e2a", "e2b", "ba", "bb",
+             "d2a", "d2b", "d1a", "d1b", "d0a", "d0b", "head")
+
+    def __init__(self, ch=(16, 48, 96, 192), seed=0, device="cuda"):
+        c0, c1, c2, c3 = ch
+        for c in ch:
+            if c % 16:
+                raise ValueError("channel counts must be multiples of 16")
+        rng = np.random.default_rng(seed)
+        spec = {"e0a": (N_IN, c0), "e0b": (c0, c0), "e1a": (c0, c1), "e1b": (c1, c1),
+                "e2a": (c1, c2), "e2b": (c2, c2), "ba": (c2, c3), "bb": (c3, c3),
+                "d2a": (c3 + c2, c2), "d2b": (c2, c2), "d1a": (c2 + c1, c1), "d1b": (c1, c1),
+                "d0a": (c1 + c0, c0), "d0b": (c0, c0)}
+        self.L = {k: Conv(ci, co, rng, device=device) for k, (ci, co) in spec.items()}
+        self.L["head"] = Conv(c0, N_OUT, rng, taps=1, relu=False, device=device, scale=0.1)
+        self.ch = ch
+        self.t = 0
+        self._saved = None
+
+    def n_params(self):
+        return sum(c.n_params() for c in self.L.values())
+
+    @staticmethod
+    def _pool(x):
+        n, d, h, w, c = x.shape
+        y = torch.empty((n, d // 2, h // 2, w // 2, c), dtype=torch.bfloat16, device=x.device)
+        nn.pool2(x, y)
+        return y
+
+    @staticmethod
+    def _up_cat(x, skip):
+        n, d, h, w, c = skip.shape
+        u = torch.empty((n, d, h, w, x.shape[-1]), dtype=torch.bfloat16, device=x.device)
+        nn.up2(x, u)
+        y = torch.empty((n, d, h, w, x.shape[-1] + c), dtype=torch.bfloat16, device=x.device)
+        nn.concat(u, skip, y)
+        return y
+
+    def forward(self, x):
+        """x: BF16 (n, B, B, B, 16), B a multiple of 8.  Returns FP32 (n, B, B, B, 16)."""
+        L = self.L
+        e0 = L["e0b"].forward(L["e0a"].forward(x))
+        e1 = L["e1b"].forward(L["e1a"].forward(self._pool(e0)))
+        e2 = L["e2b"].forward(L["e2a"].forward(self._pool(e1)))
+        b = L["bb"].forward(L["ba"].forward(self._pool(e2)))
+        d2 = L["d2b"].forward(L["d2a"].forward(self._up_cat(b, e2)))
+        d1 = L["d1b"].forward(L["d1a"].forward(self._up_cat(d2, e1)))
+        d0 = L["d0b"].forward(L["d0a"].forward(self._up_cat(d1, e0)))
+        self._saved = (e0, e1, e2, b, d2, d1)
+        return L["head"].forward(d0, out_f32=True)
+
+    @staticmethod
+    def _split_up(g, x_shape, skip_grad):
+        """Gradient of concat(up2(x), skip): returns dx and writes the skip part."""
+        n, d, h, w, _ = skip_grad.shape
+        gu = torch.empty((n, d, h, w, x_shape[-1]), dtype=torch.bfloat16, device=g.device)
+        nn.split(g, gu, skip_grad)
+        gx = torch.empty(x_shape, dtype=torch.bfloat16, device=g.device)
+        nn.up2_backward(gu, gx)
+        return gx
+
+    @staticmethod
+    def _pool_back_add(g, acc):
+        tmp = torch.empty(acc.shape, dtype=torch.bfloat16, device=g.device)
+        nn.pool2_backward(g, tmp)
+        nn.add_(acc, tmp)
+
+    def backward(self, dout):
+        """dout: BF16 gradient of the loss w.r.t. the FP32 output; accumulates the
+        weight gradients of every layer."""
+        L = self.L
+        e0, e1, e2, b, d2, d1 = self._saved
+        g = L["d0a"].backward(L["d0b"].backward(L["head"].backward(dout)))
+        ge0 = torch.empty_like(e0)
+        g = self._split_up(g, d1.shape, ge0)
+        g = L["d1a"].backward(L["d1b"].backward(g))
+        ge1 = torch.empty_like(e1)
+        g = self._split_up(g, d2.shape, ge1)
+        g = L["d2a"].backward(L["d2b"].backward(g))
+        ge2 = torch.empty_like(e2)
+        g = self._split_up(g, b.shape, ge2)
+        g = L["ba"].backward(L["bb"].backward(g))
+        self._pool_back_add(g, ge2)
+        g = L["e2a"].backward(L["e2b"].backward(ge2))
+        self._pool_back_add(g, ge1)
+        g = L["e1a"].backward(L["e1b"].backward(ge1))
+        self._pool_back_add(g, ge0)
+        L["e0a"].backward(L["e0b"].backward(ge0), need_dx=False)
+        self._saved = None
+
+    def zero_grad(self):
+        for c in self.L.values():
+            c.zero_grad()
+
+    def step(self, lr):
+        self.t += 1
+        for c in self.L.values():
+            c.step(lr, self.t)
+
+    def state(self):
+        return {k: c.state() for k, c in self.L.items()}
+
+    def load(self, st):
+        for k, c in self.L.items():
+            c.load(st[k])
+
+
+# ---------------------------------------------------------------------------
+# dataset, training, prediction
+# ---------------------------------------------------------------------------
+def generate(samples, box: int, average: bool = True, log=None):
+    """Solve every sample with the plain FP64 solver; returns (Grids, records)."""
+    grids = Grids(len(samples), box)
+    recs = []
+    t0 = time.perf_counter()
+    for i, smp in enumerate(samples):
+        g = smp.geometry()
+        ur = smp.u_ref(g)
+        runner = SteadyRunner(smp.case(g), ur)
+        try:
+            rec, rho, u = runner.run(average=average)
+        finally:
+            runner.close()
+        rec.update({"sites": int(g.n_fluid), "u_ref": ur, "kind": smp.kind, "tau": smp.tau,
+                    "drho": smp.drho})
+        grids.put(i, g, smp, runner.coords, rho, u, ur)
+        recs.append(rec)
+        if log and (i + 1) % 100 == 0:
+            log("generated %d/%d samples in %.1f s" % (i + 1, len(samples), time.perf_counter() - t0))
+    return grids, recs
+
+
+def train(net: UNet, grids: Grids, n: int, batch: int = 4, seconds: float = 600.0,
+          max_epochs: int = 1000, lr_max: float = 1e-3, lr_min: float = 2e-5, seed: int = 0, log=None):
+    """Adam on the masked MSE of the normalised targets, cosine learning-rate decay
+    over the time budget.  Returns the loss history (per epoch mean)."""
+    rng = np.random.default_rng(seed)
+    hist = []
+    t0 = time.perf_counter()
+    epoch = 0
+    done = False
+    while not done and epoch < max_epochs:
+        order = rng.permutation(n)
+        tot, cnt = 0.0, 0
+        for k in range(0, n - batch + 1, batch):
+            frac = min(1.0, (time.perf_counter() - t0) / seconds)
+            lr = lr_min + 0.5 * (lr_max - lr_min) * (1.0 + math.cos(math.pi * frac))
+            idx = order[k:k + batch]
+            x = grids.features(idx)
+            tgt, mask = grids.targets(idx)
+            out = net.forward(x)
+            dout = torch.empty(out.shape, dtype=torch.bfloat16, device=out.device)
+            loss = nn.mse(out, tgt, mask, dout)
+            net.zero_grad()
+            net.backward(dout)
+            net.step(lr)
+            tot += loss
+            cnt += 1
+            if time.perf_counter() - t0 > seconds:
+                done = True
+                break
+        epoch += 1
+        hist.append(tot / max(cnt, 1))
+        if log:
+            log("epoch %d loss %.3e (%.0f s)" % (epoch, hist[-1], time.perf_counter() - t0))
+    return hist
+
+
+def predict(net: UNet, grids: Grids, i: int, smp: Sample, coords, u_ref: float):
+    """Prediction for sample i at the fluid sites `coords` (contiguous order):
+    (rho, u) in lattice units."""
+    out = net.forward(grids.features([i]))[0]
+    x = torch.as_tensor(coords[:, 0], device=out.device, dtype=torch.long)
+    y = torch.as_tensor(coords[:, 1], device=out.device, dtype=torch.long)
+    z = torch.as_tensor(coords[:, 2], device=out.device, dtype=torch.long)
+    v = out[x, y, z, :4].double().cpu().numpy()
+    return 1.0 + v[:, 3] * smp.drho, v[:, :3] * u_ref
+
+
+def rel_l2(a, b):
+    return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))
+
+
+def evaluate(net: UNet, samples, box: int, log=None):
+    """Held-out evaluation.  Per sample, on one context: the plain solve from rest
+    (the reference's start; its field judges the others), rest with the one-off
+    averaging, the warm start (prediction, averaging) and the warm start without
+    averaging.  Wall times include the prediction and the field upload."""
+    grids = Grids(len(samples), box, with_targets=False)
+    out = []
+    t0 = time.perf_counter()
+    for i, smp in enumerate(samples):
+        g = smp.geometry()
+        grids.put(i, g, smp)
+        ur = smp.u_ref(g)
+        runner = SteadyRunner(smp.case(g), ur)
+        try:
+            rest, rho_p, u_p = runner.run()
+            rest_avg, rho_a, u_a = runner.run(average=True)
+            pred = lambda co: predict(net, grids, i, smp, co, ur)
+            warm, rho_w, u_w = runner.run(start=pred, average=True)
+            warm_plain, rho_wp, u_wp = runner.run(start=pred, average=False)
+            rho0, u0 = pred(runner.coords)
+        finally:
+            runner.close()
+        dp = lambda r: (r - 1.0) / smp.drho
+        rec = {"sample": i, "kind": smp.kind, "tau": smp.tau, "drho": smp.drho, "sites": int(g.n_fluid),
+               "u_ref": ur, "rest": rest, "rest_avg": rest_avg, "warm": warm, "warm_plain": warm_plain,
+               "prediction_u_rel_l2": rel_l2(u0, u_p), "prediction_p_rel_l2": rel_l2(dp(rho0), dp(rho_p)),
+               "warm_u_rel_l2": rel_l2(u_w, u_p), "warm_p_rel_l2": rel_l2(dp(rho_w), dp(rho_p)),
+               "rest_avg_u_rel_l2": rel_l2(u_a, u_p), "warm_plain_u_rel_l2": rel_l2(u_wp, u_p)}
+        out.append(rec)
+        if log and (i + 1) % 25 == 0:
+            log("evaluated %d/%d (%.1f s)" % (i + 1, len(samples), time.perf_counter() - t0))
+    return out
+
+
+def summarise(evals) -> dict:
+    """Medians and totals over held-out samples."""
+    def col(arm, key):
+        return np.array([e[arm][key] for e in evals], dtype=np.float64)
+    res = {"n": len(evals)}
+    for arm in ("rest", "rest_avg", "warm", "warm_plain"):
+        st = col(arm, "steps")
+        ok = st > 0
+        res[arm] = {"converged": int(ok.sum()), "median_steps": float(np.median(st[ok])) if ok.any() else None,
+                    "total_steps": float(st[ok].sum()), "total_seconds": float(col(arm, "seconds").sum()),
+                    "median_seconds": float(np.median(col(arm, "seconds")))}
+    both = np.array([e["rest"]["steps"] > 0 and e["warm"]["steps"] > 0 for e in evals])
+    if both.any():
+        r = np.array([e["rest"]["steps"] for e in evals])[both]
+        w = np.array([e["warm"]["steps"] for e in evals])[both]
+        rs = np.array([e["rest"]["seconds"] for e in evals])[both]
+        ws = np.array([e["warm"]["seconds"] for e in evals])[both]
+        ra = np.array([e["rest_avg"]["steps"] for e in evals])[both]
+        res["speedup_steps_vs_rest"] = float(r.sum() / w.sum())
+        res["speedup_seconds_vs_rest"] = float(rs.sum() / ws.sum())
+        res["median_speedup_steps_vs_rest"] = float(np.median(r / w))
+        res["speedup_steps_vs_rest_avg"] = float(ra.sum() / w.sum())
+    for k in ("prediction_u_rel_l2", "prediction_p_rel_l2", "warm_u_rel_l2", "warm_p_rel_l2",
+              "rest_avg_u_rel_l2", "warm_plain_u_rel_l2"):
+        v = np.array([e[k] for e in evals])
+        res[k] = {"median": float(np.median(v)), "p90": float(np.percentile(v, 90)), "max": float(v.max())}
+    return res

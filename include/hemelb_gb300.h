@@ -172,6 +172,14 @@ int hlbg_read_gmy(const char *path, int32_t q, void **geom_handle);
  * NONE, wall sites get the normalised sum of their wall-link vectors as normal. */
 int hlbg_write_gmy(const hlbg_geometry *geom, const char *path);
 /* Access the generated geometry and its iolets (pointers stay owned by the handle). */
+/* One seeded vessel (kind 0: stenosed pipe along z; 1: bifurcation) in a fixed box
+ * of box_sites^3 voxels (box_sites a multiple of 8), inlet on the plane z = 1.5
+ * and outlets at the far ends, bounce-back walls: the warm-start surrogate's
+ * training and held-out geometries.  No reference counterpart. */
+int hlbg_synth_vessel_box(uint64_t seed, int32_t box_sites, int32_t kind, int32_t q, void **handle);
+/* Signed distance to the wall (positive inside) at every voxel centre of the
+ * geometry's box, x slowest and z fastest (box_x * box_y * box_z floats). */
+int hlbg_synth_distance(void *handle, float *out);
 int hlbg_synth_view(void *geom_handle, hlbg_geometry *out, int64_t *n_fluid_sites,
                     int32_t *n_inlets, int32_t *n_outlets);
 int hlbg_synth_iolet(void *geom_handle, int32_t is_outlet, int32_t index, double position[3],
@@ -213,6 +221,25 @@ int hlbg_sync(hlbg_ctx *ctx);
  * captured once per step count and replayed (launch-bound small geometries and
  * batched ensembles). */
 int hlbg_step_graph(hlbg_ctx *ctx, int32_t nsteps);
+/* Step until the state is steady: StabilityTester's convergence test, max over
+ * sites of |u_new - u_old| / u_ref <= tol, checked on the device after every step
+ * (Code/lb/StabilityTester.h:91-183 with doConvergenceCheck, and the termination
+ * on convergence of SimulationMaster).  Steps run as graph launches of check_batch
+ * (1..1024) steps; the host reads the result after each, so steps_run exceeds
+ * steps_to_steady by less than check_batch.  Returns HLBG_OK when converged,
+ * HLBG_ERR_UNSTABLE when a distribution turned non-positive, HLBG_ERR_TIMEOUT
+ * after max_steps; final_rel_du is the last check's max |du| / u_ref. */
+int hlbg_run_to_steady(hlbg_ctx *ctx, double tol, double u_ref, int64_t max_steps,
+                       int32_t check_batch, int64_t *steps_to_steady, int64_t *steps_run,
+                       double *final_rel_du);
+/* Replace the current distributions by the mean of the two time levels (valid
+ * right after a step, when both arrays hold consecutive states).  No reference
+ * counterpart: applied once after the first step of a start from a prescribed
+ * field, it removes the period-two staggered-momentum component that D3Q19 with
+ * bounce-back walls conserves everywhere except at iolets (sum over sites of
+ * (-1)^(z+t) j_z, and likewise for x and y), which otherwise decays only through
+ * the iolets and dominates the time to steady state. */
+int hlbg_average_time_levels(hlbg_ctx *ctx);
 /* Autotuner: time each launch shape / schedule of the stream-and-collide kernel
  * (threads per CTA x resident CTAs per SM, per-slot grid or persistent grid) on
  * this context for steps_per_trial steps and keep the fastest.  Advances the

@@ -96,3 +96,79 @@ def adam_step(w, g, m, v, lr, step, b1=0.9, b2=0.999, eps=1e-8):
     mh = m / (1 - b1 ** step)
     vh = v / (1 - b2 ** step)
     return w - lr * mh / (np.sqrt(vh) + eps), m, v
+
+
+# ---------------------------------------------------------------------------
+# the surrogate's U-Net (hemelb_gb300.surrogate.UNet), forward and backward,
+# with the BF16 roundings of the GPU path at the same points when rnd=True
+# ---------------------------------------------------------------------------
+def bf16(a):
+    """Round to the nearest BF16 value (ties to even), returned as FP64."""
+    a = np.asarray(a, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+UNET_LAYERS = ("e0a", "e0b", "e1a", "e1b", "e2a", "e2b", "ba", "bb",
+               "d2a", "d2b", "d1a", "d1b", "d0a", "d0b", "head")
+
+
+def unet_forward(P, x, rnd=True):
+    """P: name -> (w (taps, cout, cin), b); x (n, B, B, B, cin).  Returns (out, cache)."""
+    R = bf16 if rnd else (lambda a: a)
+    cache = {}
+
+    def conv(name, a, relu=True, last=False):
+        w, b = P[name]
+        y = conv3d(a, w, b, relu=relu)
+        cache[name] = (a, y if last else R(y))
+        return y if last else R(y)
+
+    def pool(a):
+        return R(pool2(a))
+
+    e0 = conv("e0b", conv("e0a", x))
+    e1 = conv("e1b", conv("e1a", pool(e0)))
+    e2 = conv("e2b", conv("e2a", pool(e1)))
+    b = conv("bb", conv("ba", pool(e2)))
+    d2 = conv("d2b", conv("d2a", np.concatenate([up2(b), e2], axis=-1)))
+    d1 = conv("d1b", conv("d1a", np.concatenate([up2(d2), e1], axis=-1)))
+    d0 = conv("d0b", conv("d0a", np.concatenate([up2(d1), e0], axis=-1)))
+    out = conv("head", d0, relu=False, last=True)
+    cache["shapes"] = (e0.shape, e1.shape, e2.shape, b.shape, d2.shape, d1.shape)
+    return out, cache
+
+
+def unet_backward(P, cache, dout, rnd=True):
+    """Weight and bias gradients (name -> (dw, db)) for the output gradient dout."""
+    R = bf16 if rnd else (lambda a: a)
+    G = {}
+
+    def back(name, dy, relu=True, need_dx=True):
+        a, y = cache[name]
+        w, _ = P[name]
+        if relu:
+            dy = dy * (y > 0)
+        G[name] = (conv3d_weight_grad(a, dy, taps=w.shape[0]), dy.reshape(-1, dy.shape[-1]).sum(axis=0))
+        return R(conv3d_data_grad(dy, w)) if need_dx else None
+
+    s0, s1, s2, sb, sd2, sd1 = cache["shapes"]
+
+    def split_up(g, c_up):
+        return R(up2_backward(g[..., :c_up])), g[..., c_up:]
+
+    g = back("d0a", back("d0b", back("head", dout, relu=False)))
+    g, ge0 = split_up(g, sd1[-1])
+    g = back("d1a", back("d1b", g))
+    g, ge1 = split_up(g, sd2[-1])
+    g = back("d2a", back("d2b", g))
+    g, ge2 = split_up(g, sb[-1])
+    g = back("ba", back("bb", g))
+    ge2 = R(ge2 + R(pool2_backward(g)))
+    g = back("e2a", back("e2b", ge2))
+    ge1 = R(ge1 + R(pool2_backward(g)))
+    g = back("e1a", back("e1b", ge1))
+    ge0 = R(ge0 + R(pool2_backward(g)))
+    back("e0a", back("e0b", ge0), need_dx=False)
+    return G

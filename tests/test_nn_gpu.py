@@ -132,3 +132,25 @@ def test_masked_mse_and_adam():
     torch.cuda.synchronize()
     assert np.allclose(tw.double().cpu().numpy(), wr, rtol=1e-6, atol=1e-6)
     assert torch.equal(wb, tw.to(torch.bfloat16))
+
+
+def test_unet_forward_and_gradients_match_oracle():
+    """The whole U-Net (BF16 kernels, FP32 accumulation) against the oracle's U-Net
+    with the same BF16 roundings: output and every weight and bias gradient."""
+    from hemelb_gb300.surrogate import N_IN, UNet
+    net = UNet(ch=(16, 16, 32, 16), seed=1)
+    rng = np.random.default_rng(0)
+    x, xt = bf16(rng.standard_normal((1, 16, 16, 16, N_IN)))
+    out = net.forward(xt)
+    dout, doutt = bf16(rng.standard_normal(tuple(out.shape)))
+    net.zero_grad()
+    net.backward(doutt)
+    torch.cuda.synchronize()
+    P = {k: (c.wb.float().cpu().numpy().astype(np.float64), c.b.cpu().numpy().astype(np.float64))
+         for k, c in net.L.items()}
+    ref, cache = O.unet_forward(P, x)
+    assert close(out.cpu().numpy(), ref, 1e-2)
+    G = O.unet_backward(P, cache, dout)
+    for k, c in net.L.items():
+        assert close(c.gw.cpu().numpy(), G[k][0], 2e-2), k
+        assert close(c.gb.cpu().numpy(), G[k][1], 2e-2), k
