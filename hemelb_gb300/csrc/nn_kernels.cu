@@ -194,6 +194,223 @@ __global__ void __launch_bounds__(128) k_conv3d_wgrad(const __nv_bfloat16* __res
     }
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient of a 3x3x3 convolution, tiled through shared memory.
+// A CTA owns a (16 C_out) x (16 NCI C_in) block of dW for all 27 taps and runs
+// over a range of 4x4x8 voxel bricks: per brick it stages dY (128 voxels x 16 co)
+// and X on the brick plus a one-voxel halo (6x6x10 voxels x 16 NCI ci) with
+// cp.async (zero fill outside the volume), then each of the 8 warps accumulates
+// its taps (warp, warp + 8, warp + 16, warp + 24) as
+//   dW[tap] += dY^T (16 co x 16 voxels) * X_shifted (16 voxels x 8 ci)
+// on mma.sync with both operands read by ldmatrix.trans (rows of 16 bytes; the
+// row pitches of 48/80 bytes put the 8 rows of one ldmatrix in distinct banks).
+// The FP32 accumulators are added to dW once per CTA (red.global.add).
+// ---------------------------------------------------------------------------
+constexpr int kBZ = 4, kBY = 4, kBX = 8, kBV = kBZ * kBY * kBX;  // brick
+constexpr int kHZ = kBZ + 2, kHY = kBY + 2, kHX = kBX + 2, kHV = kHZ * kHY * kHX;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool ok) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int sz = ok ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t* r, const void* smem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(s));
+}
+__device__ __forceinline__ void red_add(float* p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;\n" ::"l"(p), "f"(v) : "memory");
+}
+
+template <int NCI>
+__global__ void __launch_bounds__(256) k_wgrad_brick(const __nv_bfloat16* __restrict__ x, int Cin,
+                                                      const __nv_bfloat16* __restrict__ dy, int Cout,
+                                                      float* __restrict__ dw, int D, int H, int W, int nbz,
+                                                      int nby, int nbx, int64_t nbricks, int bricks_per_cta) {
+  constexpr int CIB = 16 * NCI, XS = CIB + 8, DS = 16 + 8, NTILE = 2 * NCI;
+  __shared__ __align__(16) __nv_bfloat16 Xs[kHV * XS];
+  __shared__ __align__(16) __nv_bfloat16 Ds[kBV * DS];
+  const int co0 = blockIdx.y * 16, ci0 = blockIdx.z * CIB;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = lane >> 3, rr = lane & 7;
+  float acc[4][NTILE][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int nt = 0; nt < NTILE; ++nt) acc[j][nt][0] = acc[j][nt][1] = acc[j][nt][2] = acc[j][nt][3] = 0.f;
+  const int64_t b0 = (int64_t)blockIdx.x * bricks_per_cta;
+  const int64_t b1 = b0 + bricks_per_cta < nbricks ? b0 + bricks_per_cta : nbricks;
+  for (int64_t b = b0; b < b1; ++b) {
+    const int bx = (int)(b % nbx);
+    int64_t r = b / nbx;
+    const int by = (int)(r % nby);
+    r /= nby;
+    const int bz = (int)(r % nbz);
+    const int n = (int)(r / nbz);
+    const int z0 = bz * kBZ, y0 = by * kBY, x0 = bx * kBX;
+    for (int c = threadIdx.x; c < kBV * 2; c += 256) {
+      const int v = c >> 1, part = c & 1;
+      const int z = z0 + v / (kBY * kBX), y = y0 + (v / kBX) % kBY, xx = x0 + v % kBX;
+      const bool ok = z < D && y < H && xx < W;
+      const __nv_bfloat16* src = ok ? dy + ((((int64_t)n * D + z) * H + y) * W + xx) * Cout + co0 + part * 8 : dy;
+      cp_async16(&Ds[v * DS + part * 8], src, ok);
+    }
+    for (int c = threadIdx.x; c < kHV * NTILE; c += 256) {
+      const int h = c / NTILE, part = c % NTILE;
+      const int z = z0 + h / (kHY * kHX) - 1, y = y0 + (h / kHX) % kHY - 1, xx = x0 + h % kHX - 1;
+      const bool ok = z >= 0 && z < D && y >= 0 && y < H && xx >= 0 && xx < W;
+      const __nv_bfloat16* src = ok ? x + ((((int64_t)n * D + z) * H + y) * W + xx) * Cin + ci0 + part * 8 : x;
+      cp_async16(&Xs[h * XS + part * 8], src, ok);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+#pragma unroll 1
+    for (int s = 0; s < kBV / 16; ++s) {
+      uint32_t a[4];
+      ldsm_x4_trans(a, &Ds[(16 * s + rr + ((q >> 1) << 3)) * DS + (q & 1) * 8]);
+      // the voxel whose X row this lane addresses for the B operand
+      const int vb = 16 * s + rr + ((q & 1) << 3);
+      const int vz = vb / (kBY * kBX), vy = (vb / kBX) % kBY, vx = vb % kBX;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int tap = warp + 8 * j;
+        if (tap < 27) {
+          const int h = ((vz + tap / 9) * kHY + (vy + (tap / 3) % 3)) * kHX + (vx + tap % 3);
+#pragma unroll
+          for (int nt = 0; nt < NTILE; nt += 2) {
+            uint32_t bf[4];
+            ldsm_x4_trans(bf, &Xs[h * XS + (nt + (q >> 1)) * 8]);
+            mma_bf16(acc[j][nt], a, bf);
+            mma_bf16(acc[j][nt + 1], a, bf + 2);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int tap = warp + 8 * j;
+    if (tap < 27) {
+#pragma unroll
+      for (int nt = 0; nt < NTILE; ++nt)
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+          for (int e = 0; e < 2; ++e)
+            red_add(dw + ((int64_t)tap * Cout + co0 + g + 8 * hh) * Cin + ci0 + nt * 8 + 2 * t + e,
+                    acc[j][nt][2 * hh + e]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3x3x3 convolution tiled through shared memory.  A CTA computes one 4x4x8 voxel
+// brick (8 warps x 16 voxels) for 16 NCO output channels.  For each 16-channel
+// slice of the input it stages X on the brick plus halo (6x6x10 voxels) with
+// cp.async (zero fill outside the volume), and for each plane of 9 taps the
+// weights W[tap][co][ci] of that slice; the warps then accumulate
+//   out (16 voxels x 8 co) += X_shifted (16 voxels x 16 ci) * W[tap]^T (16 ci x 8 co)
+// with A read by ldmatrix from the halo rows of the shifted voxels and B by
+// ldmatrix from the weight rows.  Epilogue: bias, optional ReLU, BF16 (and FP32).
+// ---------------------------------------------------------------------------
+template <int NCO>
+__global__ void __launch_bounds__(256) k_conv_brick(const __nv_bfloat16* __restrict__ in, int Cin,
+                                                     const __nv_bfloat16* __restrict__ w,
+                                                     const float* __restrict__ bias,
+                                                     __nv_bfloat16* __restrict__ out, float* __restrict__ out_f32,
+                                                     int Cout, int D, int H, int W, int nbz, int nby, int nbx,
+                                                     int relu) {
+  constexpr int COB = 16 * NCO, NTILE = 2 * NCO, XS = 24, WS = 24;
+  __shared__ __align__(16) __nv_bfloat16 Xs[kHV * XS];
+  __shared__ __align__(16) __nv_bfloat16 Ws[9 * COB * WS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = lane >> 3, rr = lane & 7;
+  const int co0 = blockIdx.y * COB;
+  int64_t r = blockIdx.x;
+  const int bx = (int)(r % nbx);
+  r /= nbx;
+  const int by = (int)(r % nby);
+  r /= nby;
+  const int bz = (int)(r % nbz);
+  const int n = (int)(r / nbz);
+  const int z0 = bz * kBZ, y0 = by * kBY, x0 = bx * kBX;
+  float acc[NTILE][4];
+#pragma unroll
+  for (int nt = 0; nt < NTILE; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+  // this lane's A row: voxel 16 warp + rr + 8 (q & 1) of the brick, channel half q >> 1
+  const int va = 16 * warp + rr + ((q & 1) << 3);
+  const int az = va / (kBY * kBX), ay = (va / kBX) % kBY, ax = va % kBX;
+  for (int ci0 = 0; ci0 < Cin; ci0 += 16) {
+    for (int c = threadIdx.x; c < kHV * 2; c += 256) {
+      const int h = c >> 1, part = c & 1;
+      const int z = z0 + h / (kHY * kHX) - 1, y = y0 + (h / kHX) % kHY - 1, xx = x0 + h % kHX - 1;
+      const bool ok = z >= 0 && z < D && y >= 0 && y < H && xx >= 0 && xx < W;
+      const __nv_bfloat16* src = ok ? in + ((((int64_t)n * D + z) * H + y) * W + xx) * Cin + ci0 + part * 8 : in;
+      cp_async16(&Xs[h * XS + part * 8], src, ok);
+    }
+#pragma unroll 1
+    for (int plane = 0; plane < 3; ++plane) {
+      for (int c = threadIdx.x; c < 9 * COB * 2; c += 256) {
+        const int row = c >> 1, part = c & 1;  // row = tap-in-plane * COB + co
+        const int tp = row / COB, co = row % COB;
+        const __nv_bfloat16* src = w + ((int64_t)(plane * 9 + tp) * Cout + co0 + co) * Cin + ci0 + part * 8;
+        cp_async16(&Ws[row * WS + part * 8], src, true);
+      }
+      cp_async_wait_all();
+      __syncthreads();
+#pragma unroll
+      for (int tp = 0; tp < 9; ++tp) {
+        const int h = ((az + plane) * kHY + (ay + tp / 3)) * kHX + (ax + tp % 3);
+        uint32_t a[4];
+        {
+          const unsigned sa = (unsigned)__cvta_generic_to_shared(&Xs[h * XS + (q >> 1) * 8]);
+          asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                       : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+                       : "r"(sa));
+        }
+#pragma unroll
+        for (int nt = 0; nt < NTILE; nt += 2) {
+          uint32_t b[4];
+          const unsigned sb =
+              (unsigned)__cvta_generic_to_shared(&Ws[(tp * COB + (nt + (q >> 1)) * 8 + rr) * WS + (q & 1) * 8]);
+          asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                       : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3])
+                       : "r"(sb));
+          mma_bf16(acc[nt], a, b);
+          mma_bf16(acc[nt + 1], a, b + 2);
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // epilogue: rows g and g + 8 of the warp's 16 voxels, columns 2t, 2t + 1 of each tile
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int hh = 0; hh < 2; ++hh) {
+    const int v = 16 * warp + g + 8 * hh;
+    const int z = z0 + v / (kBY * kBX), y = y0 + (v / kBX) % kBY, xx = x0 + v % kBX;
+    if (z >= D || y >= H || xx >= W) continue;
+    const int64_t m = (((int64_t)n * D + z) * H + y) * W + xx;
+#pragma unroll
+    for (int nt = 0; nt < NTILE; ++nt)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int co = co0 + nt * 8 + 2 * t + e;
+        float vv = acc[nt][2 * hh + e] + (bias ? bias[co] : 0.f);
+        if (relu && vv < 0.f) vv = 0.f;
+        out[m * Cout + co] = __float2bfloat16_rn(vv);
+        if (out_f32) out_f32[m * Cout + co] = vv;
+      }
+  }
+}
+
 // Flipped, transposed weights for the data-gradient convolution:
 // wt[26 - tap][ci][co] = w[tap][co][ci]
 __global__ void k_flip_transpose(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __restrict__ wt,
@@ -350,6 +567,24 @@ int hlbg_nn_conv3d(const void* in, int32_t cin, const void* w, const float* bias
   if (!in || !w || !out || cin <= 0 || cin % 16 || cout <= 0 || (taps != 27 && taps != 1)) return 1;
   const int64_t M = (int64_t)n * d * h * wd;
   cudaStream_t st = (cudaStream_t)stream;
+  if (taps == 27 && cout % 16 == 0) {
+    const int nbz = (d + kBZ - 1) / kBZ, nby = (h + kBY - 1) / kBY, nbx = (wd + kBX - 1) / kBX;
+    const int64_t nbricks = (int64_t)n * nbz * nby * nbx;
+    auto I = (const __nv_bfloat16*)in;
+    auto Wt = (const __nv_bfloat16*)w;
+    auto O = (__nv_bfloat16*)out;
+    if (cout % 64 == 0) {
+      dim3 grid((unsigned)nbricks, (unsigned)(cout / 64));
+      k_conv_brick<4><<<grid, 256, 0, st>>>(I, cin, Wt, bias, O, out_f32, cout, d, h, wd, nbz, nby, nbx, relu);
+    } else if (cout % 32 == 0) {
+      dim3 grid((unsigned)nbricks, (unsigned)(cout / 32));
+      k_conv_brick<2><<<grid, 256, 0, st>>>(I, cin, Wt, bias, O, out_f32, cout, d, h, wd, nbz, nby, nbx, relu);
+    } else {
+      dim3 grid((unsigned)nbricks, (unsigned)(cout / 16));
+      k_conv_brick<1><<<grid, 256, 0, st>>>(I, cin, Wt, bias, O, out_f32, cout, d, h, wd, nbz, nby, nbx, relu);
+    }
+    return check_launch();
+  }
   const int warps = (int)((M + 15) / 16);
   dim3 grid((unsigned)((warps + 3) / 4), 1);
   auto I = (const __nv_bfloat16*)in;
@@ -368,6 +603,25 @@ int hlbg_nn_conv3d(const void* in, int32_t cin, const void* w, const float* bias
 int hlbg_nn_conv3d_wgrad(const void* x, int32_t cin, const void* dy, int32_t cout, float* dw, int32_t n,
                          int32_t d, int32_t h, int32_t wd, int32_t taps, void* stream) {
   if (!x || !dy || !dw || cin % 8 || cout <= 0) return 1;
+  if (taps == 27 && cin % 16 == 0 && cout % 16 == 0) {
+    const int nbz = (d + kBZ - 1) / kBZ, nby = (h + kBY - 1) / kBY, nbx = (wd + kBX - 1) / kBX;
+    const int64_t nbricks = (int64_t)n * nbz * nby * nbx;
+    const int nci = cin % 32 == 0 ? 2 : 1;
+    const int gy = cout / 16, gz = cin / (16 * nci);
+    // about four waves of 2 CTAs per SM over 152 SMs
+    int64_t bpc = (nbricks * gy * gz + 1215) / 1216;
+    if (bpc < 1) bpc = 1;
+    dim3 grid((unsigned)((nbricks + bpc - 1) / bpc), (unsigned)gy, (unsigned)gz);
+    auto X = (const __nv_bfloat16*)x;
+    auto DY = (const __nv_bfloat16*)dy;
+    if (nci == 2)
+      k_wgrad_brick<2><<<grid, 256, 0, (cudaStream_t)stream>>>(X, cin, DY, cout, dw, d, h, wd, nbz, nby, nbx,
+                                                                nbricks, (int)bpc);
+    else
+      k_wgrad_brick<1><<<grid, 256, 0, (cudaStream_t)stream>>>(X, cin, DY, cout, dw, d, h, wd, nbz, nby, nbx,
+                                                                nbricks, (int)bpc);
+    return check_launch();
+  }
   const int64_t M = (int64_t)n * d * h * wd;
   const int64_t ntile = (int64_t)taps * ((cout + 15) / 16) * (cin / 8);
   const int64_t slice = 4096;

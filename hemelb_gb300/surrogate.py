@@ -100,11 +100,13 @@ class SteadyRunner:
                 self.s.DoTimeStep(1)
             self.s.RunToSteady(tol, u_ref, check_batch, check_batch)
 
-    def run(self, start=None, average: bool = False, max_steps: int = 400_000):
+    def run(self, start=None, average: bool = False, max_steps: int = 400_000, timed: bool = True):
         """From rest (start None) or from the equilibrium on start(coords) -> (rho, u)
-        in contiguous site order.  Returns (record, rho, u) of the final state."""
+        in contiguous site order.  Returns (record, rho, u) of the final state.  A
+        timed run first waits for all device work, so its clock covers only itself."""
         s = self.s
-        torch.cuda.synchronize()
+        if timed:
+            torch.cuda.synchronize()
         t0 = time.perf_counter()
         if start is None:
             s.SetInitialConditions()
@@ -145,11 +147,17 @@ class Grids:
         c = (torch.arange(box, dtype=torch.float32, device=device) + 0.5) / box - 0.5
         self.coord = torch.stack(torch.meshgrid(c, c, c, indexing="ij"), dim=-1)  # (B, B, B, 3)
 
-    def put(self, i: int, g: SyntheticGeometry, smp: Sample, coords=None, rho=None, u=None, u_ref=None):
-        fl = g.fluid_grid()
-        self.mask[i] = torch.from_numpy(fl.astype(np.uint8)).to(self.mask.device)
-        sd = np.clip(g.signed_distance() / 8.0, -2.0, 2.0)
-        self.sdf[i] = torch.from_numpy(sd.astype(np.float16)).to(self.sdf.device)
+    @staticmethod
+    def host_inputs(g: SyntheticGeometry):
+        """(fluid mask uint8, scaled signed distance FP16) on the box grid."""
+        sd = np.clip(g.signed_distance() / 8.0, -2.0, 2.0).astype(np.float16)
+        return g.fluid_grid().astype(np.uint8), sd
+
+    def put(self, i: int, g: SyntheticGeometry | None, smp: Sample, coords=None, rho=None, u=None,
+            u_ref=None, inputs=None):
+        fl, sd = inputs if inputs is not None else self.host_inputs(g)
+        self.mask[i] = torch.from_numpy(fl).to(self.mask.device)
+        self.sdf[i] = torch.from_numpy(sd).to(self.sdf.device)
         self.scal[i, 0] = (smp.drho - 1.75e-3) / 1.25e-3
         self.scal[i, 1] = (smp.tau - 0.85) / 0.15
         if coords is not None and self.target is not None:
@@ -355,25 +363,34 @@ class UNet:
 # ---------------------------------------------------------------------------
 # dataset, training, prediction
 # ---------------------------------------------------------------------------
-def generate(samples, box: int, average: bool = True, log=None):
-    """Solve every sample with the plain FP64 solver; returns (Grids, records)."""
+def _solve_sample(smp: Sample, average: bool):
+    g = smp.geometry()
+    ur = smp.u_ref(g)
+    runner = SteadyRunner(smp.case(g), ur)
+    try:
+        rec, rho, u = runner.run(average=average, timed=False)
+    finally:
+        runner.close()
+    rec.update({"sites": int(g.n_fluid), "u_ref": ur, "kind": smp.kind, "tau": smp.tau, "drho": smp.drho})
+    return rec, runner.coords, rho, u, Grids.host_inputs(g)
+
+
+def generate(samples, box: int, average: bool = True, workers: int = 8, log=None):
+    """Solve every sample with the plain FP64 solver, `workers` contexts at a time
+    (one host thread and CUDA stream each: a single small geometry leaves most of
+    the GPU idle).  Returns (Grids, records)."""
+    from concurrent.futures import ThreadPoolExecutor
     grids = Grids(len(samples), box)
-    recs = []
+    recs = [None] * len(samples)
     t0 = time.perf_counter()
-    for i, smp in enumerate(samples):
-        g = smp.geometry()
-        ur = smp.u_ref(g)
-        runner = SteadyRunner(smp.case(g), ur)
-        try:
-            rec, rho, u = runner.run(average=average)
-        finally:
-            runner.close()
-        rec.update({"sites": int(g.n_fluid), "u_ref": ur, "kind": smp.kind, "tau": smp.tau,
-                    "drho": smp.drho})
-        grids.put(i, g, smp, runner.coords, rho, u, ur)
-        recs.append(rec)
-        if log and (i + 1) % 100 == 0:
-            log("generated %d/%d samples in %.1f s" % (i + 1, len(samples), time.perf_counter() - t0))
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        futs = [ex.submit(_solve_sample, smp, average) for smp in samples]
+        for i, (smp, f) in enumerate(zip(samples, futs)):
+            rec, co, rho, u, inputs = f.result()
+            grids.put(i, None, smp, co, rho, u, rec["u_ref"], inputs=inputs)
+            recs[i] = rec
+            if log and (i + 1) % 250 == 0:
+                log("generated %d/%d samples in %.1f s" % (i + 1, len(samples), time.perf_counter() - t0))
     return grids, recs
 
 

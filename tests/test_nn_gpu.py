@@ -21,11 +21,13 @@ def close(got, ref, rel):
     return np.abs(got - ref).max() <= rel * np.abs(ref).max() + 1e-6
 
 
-@pytest.mark.parametrize("cin,cout,taps,relu", [(16, 32, 27, False), (32, 48, 27, True), (16, 4, 1, False),
-                                                (48, 16, 27, False), (16, 8, 27, True)])
-def test_conv_forward(cin, cout, taps, relu):
+@pytest.mark.parametrize("cin,cout,taps,relu,shape", [
+    (16, 32, 27, False, (2, 6, 5, 7)), (32, 48, 27, True, (2, 6, 5, 7)), (16, 4, 1, False, (2, 6, 5, 7)),
+    (48, 16, 27, False, (2, 6, 5, 7)), (16, 8, 27, True, (2, 6, 5, 7)), (16, 64, 27, True, (2, 6, 5, 7)),
+    (32, 64, 27, False, (1, 13, 20, 24)), (48, 96, 27, True, (1, 9, 12, 17))])
+def test_conv_forward(cin, cout, taps, relu, shape):
+    """Shapes with partial 4x4x8 bricks at the volume edges, and volumes of many bricks."""
     rng = np.random.default_rng(cin + cout)
-    shape = (2, 6, 5, 7)
     x, xt = bf16(rng.standard_normal(shape + (cin,)))
     w, wt = bf16(rng.standard_normal((taps, cout, cin)) / np.sqrt(27 * cin))
     b = rng.standard_normal(cout).astype(np.float32)
@@ -40,10 +42,10 @@ def test_conv_forward(cin, cout, taps, relu):
     assert np.all(np.abs(y.float().cpu().numpy() - y32.cpu().numpy()) <= 2.0 ** -8 * np.abs(y32.cpu().numpy()) + 1e-30)
 
 
-@pytest.mark.parametrize("cin,cout", [(16, 32), (32, 16), (48, 48)])
-def test_conv_gradients(cin, cout):
+@pytest.mark.parametrize("cin,cout,shape", [(16, 32, (2, 6, 5, 4)), (32, 16, (2, 6, 5, 4)), (48, 48, (2, 6, 5, 4)),
+                                             (32, 32, (2, 13, 20, 24)), (16, 48, (1, 9, 12, 17))])
+def test_conv_gradients(cin, cout, shape):
     rng = np.random.default_rng(7 + cin)
-    shape = (2, 6, 5, 4)
     x, xt = bf16(rng.standard_normal(shape + (cin,)))
     w, wt = bf16(rng.standard_normal((27, cout, cin)) / np.sqrt(27 * cin))
     dy, dyt = bf16(rng.standard_normal(shape + (cout,)))
@@ -135,22 +137,34 @@ def test_masked_mse_and_adam():
 
 
 def test_unet_forward_and_gradients_match_oracle():
-    """The whole U-Net (BF16 kernels, FP32 accumulation) against the oracle's U-Net
-    with the same BF16 roundings: output and every weight and bias gradient."""
+    """The whole U-Net (BF16 kernels, FP32 accumulation) against the oracle's U-Net.
+    Forward: every layer's BF16 output against the oracle convolution of the same
+    layer input, within one BF16 rounding.  Backward: the oracle's backward pass on
+    the GPU's own activations (so both see the same ReLU masks; a mask flip near
+    zero would change a gradient by O(1) and is a property of BF16, not of the
+    kernels), against every weight and bias gradient."""
     from hemelb_gb300.surrogate import N_IN, UNet
     net = UNet(ch=(16, 16, 32, 16), seed=1)
     rng = np.random.default_rng(0)
     x, xt = bf16(rng.standard_normal((1, 16, 16, 16, N_IN)))
     out = net.forward(xt)
+    torch.cuda.synchronize()
+    acts = {k: (c.x.float().cpu().numpy().astype(np.float64), c.y.float().cpu().numpy().astype(np.float64))
+            for k, c in net.L.items()}
+    P = {k: (c.wb.float().cpu().numpy().astype(np.float64), c.b.cpu().numpy().astype(np.float64))
+         for k, c in net.L.items()}
+    for k, (a, y) in acts.items():
+        w, b = P[k]
+        ref = O.conv3d(a, w, b, relu=net.L[k].relu)
+        assert np.all(np.abs(y - ref) <= 2.0 ** -8 * np.abs(ref) + 1e-6 * np.abs(ref).max()), k
+    assert close(out.cpu().numpy(), O.conv3d(*acts["head"][:1], *P["head"]), 1e-5)
     dout, doutt = bf16(rng.standard_normal(tuple(out.shape)))
     net.zero_grad()
     net.backward(doutt)
     torch.cuda.synchronize()
-    P = {k: (c.wb.float().cpu().numpy().astype(np.float64), c.b.cpu().numpy().astype(np.float64))
-         for k, c in net.L.items()}
-    ref, cache = O.unet_forward(P, x)
-    assert close(out.cpu().numpy(), ref, 1e-2)
+    cache = dict(acts)
+    cache["shapes"] = tuple(acts[k][1].shape for k in ("e0b", "e1b", "e2b", "bb", "d2b", "d1b"))
     G = O.unet_backward(P, cache, dout)
     for k, c in net.L.items():
-        assert close(c.gw.cpu().numpy(), G[k][0], 2e-2), k
-        assert close(c.gb.cpu().numpy(), G[k][1], 2e-2), k
+        assert close(c.gw.cpu().numpy(), G[k][0], 1e-2), k
+        assert close(c.gb.cpu().numpy(), G[k][1], 1e-2), k
