@@ -167,25 +167,45 @@ class Grids:
             t[x, y, z, 3] = (rho - 1.0) / smp.drho
             self.target[i] = torch.from_numpy(t).to(self.target.device)
 
-    def features(self, idx) -> torch.Tensor:
-        """BF16 input tensor (n, B, B, B, 16) for the samples idx."""
+    @staticmethod
+    def _space(t, code: int):
+        """Exact symmetries of the problem in the x-y plane (inlet plane z fixed):
+        bit 0 mirrors x, bit 1 mirrors y, bit 2 swaps x and y (dims 1 and 2)."""
+        if code & 1:
+            t = t.flip(1)
+        if code & 2:
+            t = t.flip(2)
+        if code & 4:
+            t = t.transpose(1, 2)
+        return t
+
+    def features(self, idx, code: int = 0) -> torch.Tensor:
+        """BF16 input tensor (n, B, B, B, 16) for the samples idx, transformed by `code`."""
         idx = torch.as_tensor(idx, device=self.mask.device)
         n = idx.numel()
         f = torch.zeros((n,) + (self.box,) * 3 + (N_IN,), dtype=torch.float32, device=self.mask.device)
-        f[..., 0] = self.mask[idx].float()
-        f[..., 1] = self.sdf[idx].float()
+        f[..., 0] = self._space(self.mask[idx].float(), code)
+        f[..., 1] = self._space(self.sdf[idx].float(), code)
         f[..., 2] = self.scal[idx, 0].view(n, 1, 1, 1)
         f[..., 3] = self.scal[idx, 1].view(n, 1, 1, 1)
-        f[..., 4:7] = self.coord
+        f[..., 4:7] = self.coord  # position in the box, not transformed
         return f.to(torch.bfloat16).contiguous()
 
-    def targets(self, idx):
-        """(FP32 targets padded to 16 channels, FP32 fluid mask) for the samples idx."""
+    def targets(self, idx, code: int = 0):
+        """(FP32 targets padded to 16 channels, FP32 fluid mask) for the samples idx,
+        transformed by `code` (mirrored velocity components change sign; the swap
+        exchanges u_x and u_y)."""
         idx = torch.as_tensor(idx, device=self.mask.device)
-        t = torch.zeros(self.target[idx].shape[:-1] + (N_OUT,), dtype=torch.float32,
-                        device=self.mask.device)
-        t[..., :4] = self.target[idx]
-        return t.contiguous(), self.mask[idx].float().contiguous()
+        src = self._space(self.target[idx], code)
+        t = torch.zeros(src.shape[:-1] + (N_OUT,), dtype=torch.float32, device=self.mask.device)
+        t[..., :4] = src
+        if code & 1:
+            t[..., 0] = -t[..., 0]
+        if code & 2:
+            t[..., 1] = -t[..., 1]
+        if code & 4:
+            t[..., [0, 1]] = t[..., [1, 0]]
+        return t.contiguous(), self._space(self.mask[idx].float(), code).contiguous()
 
 
 # ---------------------------------------------------------------------------
@@ -395,9 +415,11 @@ def generate(samples, box: int, average: bool = True, workers: int = 8, log=None
 
 
 def train(net: UNet, grids: Grids, n: int, batch: int = 4, seconds: float = 600.0,
-          max_epochs: int = 1000, lr_max: float = 1e-3, lr_min: float = 2e-5, seed: int = 0, log=None):
+          max_epochs: int = 1000, lr_max: float = 1e-3, lr_min: float = 2e-5, seed: int = 0,
+          augment: bool = True, log=None):
     """Adam on the masked MSE of the normalised targets, cosine learning-rate decay
-    over the time budget.  Returns the loss history (per epoch mean)."""
+    over the time budget, each batch under a random symmetry of the x-y plane when
+    `augment`.  Returns the loss history (per epoch mean)."""
     rng = np.random.default_rng(seed)
     hist = []
     t0 = time.perf_counter()
@@ -410,8 +432,9 @@ def train(net: UNet, grids: Grids, n: int, batch: int = 4, seconds: float = 600.
             frac = min(1.0, (time.perf_counter() - t0) / seconds)
             lr = lr_min + 0.5 * (lr_max - lr_min) * (1.0 + math.cos(math.pi * frac))
             idx = order[k:k + batch]
-            x = grids.features(idx)
-            tgt, mask = grids.targets(idx)
+            code = int(rng.integers(8)) if augment else 0
+            x = grids.features(idx, code)
+            tgt, mask = grids.targets(idx, code)
             out = net.forward(x)
             dout = torch.empty(out.shape, dtype=torch.bfloat16, device=out.device)
             loss = nn.mse(out, tgt, mask, dout)
@@ -445,11 +468,12 @@ def rel_l2(a, b):
     return float(np.sqrt(((a - b) ** 2).sum() / max((b ** 2).sum(), 1e-300)))
 
 
-def evaluate(net: UNet, samples, box: int, log=None):
+def evaluate(net: UNet, samples, box: int, plain_warm: int = 0, log=None):
     """Held-out evaluation.  Per sample, on one context: the plain solve from rest
     (the reference's start; its field judges the others), rest with the one-off
-    averaging, the warm start (prediction, averaging) and the warm start without
-    averaging.  Wall times include the prediction and the field upload."""
+    averaging, and the warm start (prediction, averaging); for the first
+    `plain_warm` samples also the warm start without averaging.  Wall times include
+    the prediction and the field upload."""
     grids = Grids(len(samples), box, with_targets=False)
     out = []
     t0 = time.perf_counter()
@@ -463,16 +487,21 @@ def evaluate(net: UNet, samples, box: int, log=None):
             rest_avg, rho_a, u_a = runner.run(average=True)
             pred = lambda co: predict(net, grids, i, smp, co, ur)
             warm, rho_w, u_w = runner.run(start=pred, average=True)
-            warm_plain, rho_wp, u_wp = runner.run(start=pred, average=False)
+            warm_plain = None
+            if i < plain_warm:
+                warm_plain, _, u_wp = runner.run(start=pred, average=False)
             rho0, u0 = pred(runner.coords)
         finally:
             runner.close()
         dp = lambda r: (r - 1.0) / smp.drho
         rec = {"sample": i, "kind": smp.kind, "tau": smp.tau, "drho": smp.drho, "sites": int(g.n_fluid),
-               "u_ref": ur, "rest": rest, "rest_avg": rest_avg, "warm": warm, "warm_plain": warm_plain,
+               "u_ref": ur, "rest": rest, "rest_avg": rest_avg, "warm": warm,
                "prediction_u_rel_l2": rel_l2(u0, u_p), "prediction_p_rel_l2": rel_l2(dp(rho0), dp(rho_p)),
                "warm_u_rel_l2": rel_l2(u_w, u_p), "warm_p_rel_l2": rel_l2(dp(rho_w), dp(rho_p)),
-               "rest_avg_u_rel_l2": rel_l2(u_a, u_p), "warm_plain_u_rel_l2": rel_l2(u_wp, u_p)}
+               "rest_avg_u_rel_l2": rel_l2(u_a, u_p)}
+        if warm_plain is not None:
+            rec["warm_plain"] = warm_plain
+            rec["warm_plain_u_rel_l2"] = rel_l2(u_wp, u_p)
         out.append(rec)
         if log and (i + 1) % 25 == 0:
             log("evaluated %d/%d (%.1f s)" % (i + 1, len(samples), time.perf_counter() - t0))
@@ -481,15 +510,18 @@ def evaluate(net: UNet, samples, box: int, log=None):
 
 def summarise(evals) -> dict:
     """Medians and totals over held-out samples."""
-    def col(arm, key):
-        return np.array([e[arm][key] for e in evals], dtype=np.float64)
     res = {"n": len(evals)}
     for arm in ("rest", "rest_avg", "warm", "warm_plain"):
-        st = col(arm, "steps")
+        sub = [e for e in evals if arm in e]
+        if not sub:
+            continue
+        st = np.array([e[arm]["steps"] for e in sub], dtype=np.float64)
+        secs = np.array([e[arm]["seconds"] for e in sub], dtype=np.float64)
         ok = st > 0
-        res[arm] = {"converged": int(ok.sum()), "median_steps": float(np.median(st[ok])) if ok.any() else None,
-                    "total_steps": float(st[ok].sum()), "total_seconds": float(col(arm, "seconds").sum()),
-                    "median_seconds": float(np.median(col(arm, "seconds")))}
+        res[arm] = {"n": len(sub), "converged": int(ok.sum()),
+                    "median_steps": float(np.median(st[ok])) if ok.any() else None,
+                    "total_steps": float(st[ok].sum()), "total_seconds": float(secs.sum()),
+                    "median_seconds": float(np.median(secs))}
     both = np.array([e["rest"]["steps"] > 0 and e["warm"]["steps"] > 0 for e in evals])
     if both.any():
         r = np.array([e["rest"]["steps"] for e in evals])[both]
@@ -503,6 +535,120 @@ def summarise(evals) -> dict:
         res["speedup_steps_vs_rest_avg"] = float(ra.sum() / w.sum())
     for k in ("prediction_u_rel_l2", "prediction_p_rel_l2", "warm_u_rel_l2", "warm_p_rel_l2",
               "rest_avg_u_rel_l2", "warm_plain_u_rel_l2"):
-        v = np.array([e[k] for e in evals])
+        v = np.array([e[k] for e in evals if k in e])
+        if not v.size:
+            continue
         res[k] = {"median": float(np.median(v)), "p90": float(np.percentile(v, 90)), "max": float(v.max())}
     return res
+
+
+def accuracy_study(net: UNet, samples, box: int, check_every: int = 50, log=None):
+    """Steps to the plain solve's own accuracy.  A reference field comes from the
+    plain solve continued to max |du| / U_ref <= 1e-9 (or three times its steps);
+    the plain solve's error against it is the accuracy to match.  The rest start
+    with averaging and the warm start are then stepped, checked every
+    `check_every` steps, until their error against the reference is no larger."""
+    grids = Grids(len(samples), box, with_targets=False)
+    out = []
+    for i, smp in enumerate(samples):
+        g = smp.geometry()
+        grids.put(i, g, smp)
+        ur = smp.u_ref(g)
+        runner = SteadyRunner(smp.case(g), ur)
+        s = runner.s
+        try:
+            rest, _, u_p = runner.run()
+            steps_rest = rest["steps_run"]
+            s.RunToSteady(1e-9, ur, max(3 * steps_rest, 20000), runner.check_batch)
+            u_ref_field = s.macro()[1]
+            e_plain = rel_l2(u_p, u_ref_field)
+            rec = {"sample": i, "kind": smp.kind, "tau": smp.tau, "rest_steps": steps_rest,
+                   "rest_error": e_plain}
+            pred = lambda co: predict(net, grids, i, smp, co, ur)
+            for arm, start in (("rest_avg", None), ("warm", pred)):
+                if start is None:
+                    s.SetInitialConditions()
+                else:
+                    s.SetInitialField(*start(runner.coords))
+                s.DoTimeStep(1)
+                s.AverageTimeLevels()
+                steps, err = 1, float("inf")
+                while steps < 4 * steps_rest:
+                    s.DoTimeStepGraph(check_every)
+                    steps += check_every
+                    err = rel_l2(s.macro()[1], u_ref_field)
+                    if err <= e_plain:
+                        break
+                rec[arm + "_steps_to_match"] = steps if err <= e_plain else -1
+                rec[arm + "_error"] = err
+        finally:
+            runner.close()
+        out.append(rec)
+        if log and (i + 1) % 10 == 0:
+            log("accuracy study %d/%d" % (i + 1, len(samples)))
+    ok = [r for r in out if r["warm_steps_to_match"] > 0]
+    summ = {"n": len(out), "matched": len(ok),
+            "median_rest_error": float(np.median([r["rest_error"] for r in out])),
+            "rest_steps_total": float(sum(r["rest_steps"] for r in ok)),
+            "warm_steps_to_match_total": float(sum(r["warm_steps_to_match"] for r in ok)),
+            "rest_avg_steps_to_match_total": float(sum(max(r["rest_avg_steps_to_match"], 0) for r in ok))}
+    if ok:
+        summ["speedup_at_same_accuracy_vs_rest"] = summ["rest_steps_total"] / summ["warm_steps_to_match_total"]
+        summ["median_speedup_at_same_accuracy"] = float(np.median(
+            [r["rest_steps"] / r["warm_steps_to_match"] for r in ok]))
+    return out, summ
+
+
+def main(argv=None):
+    """Generate, train, evaluate: the warm-start report as one JSON document."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--train", type=int, default=3000)
+    ap.add_argument("--test", type=int, default=300)
+    ap.add_argument("--box", type=int, default=96)
+    ap.add_argument("--train-seconds", type=float, default=900.0)
+    ap.add_argument("--batch", type=int, default=4)
+    ap.add_argument("--plain-warm", type=int, default=16)
+    ap.add_argument("--accuracy-study", type=int, default=32)
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--out", default="")
+    ap.add_argument("--save-weights", default="")
+    a = ap.parse_args(argv)
+    log = lambda m: print(m, flush=True)
+    train_s = [Sample.draw(i, box=a.box) for i in range(a.train)]
+    test_s = [Sample.draw(1_000_000 + i, box=a.box) for i in range(a.test)]
+    t0 = time.perf_counter()
+    grids, recs = generate(train_s, a.box, average=True, workers=a.workers, log=log)
+    t_gen = time.perf_counter() - t0
+    st = np.array([r["steps"] for r in recs])
+    net = UNet(seed=0)
+    t0 = time.perf_counter()
+    hist = train(net, grids, a.train, batch=a.batch, seconds=a.train_seconds, log=log)
+    t_train = time.perf_counter() - t0
+    del grids
+    torch.cuda.empty_cache()
+    evals = evaluate(net, test_s, a.box, plain_warm=a.plain_warm, log=log)
+    summ = summarise(evals)
+    acc, acc_summ = accuracy_study(net, test_s[:a.accuracy_study], a.box, log=log)
+    doc = {"workload": "%d training + %d held-out seeded stenoses/bifurcations in a %d^3 box, D3Q19 LBGK "
+                       "FP64, bounce-back walls, Nash pressure iolets" % (a.train, a.test, a.box),
+           "criterion": "max |u_new - u_old| / U_ref <= 1e-6 after every step",
+           "network": {"params": net.n_params(), "channels": list(net.ch), "dtype": "bf16, fp32 accumulate"},
+           "datagen": {"seconds": t_gen, "median_steps": float(np.median(st)), "failed": int((st < 0).sum())},
+           "training": {"seconds": t_train, "epochs": len(hist), "loss_first": hist[0], "loss_last": hist[-1]},
+           "heldout": summ, "accuracy_study": acc_summ,
+           "samples": evals, "accuracy_samples": acc}
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(doc, f, indent=1, default=float)
+    if a.save_weights:
+        np.savez_compressed(a.save_weights, **{k + "_" + n: v for k, c in net.state().items()
+                                               for n, v in c.items()})
+    log(json.dumps({k: doc[k] for k in ("network", "datagen", "training", "heldout", "accuracy_study")},
+                   indent=1, default=float))
+    return doc
+
+
+if __name__ == "__main__":
+    main()
