@@ -289,6 +289,8 @@ def main():
     t_layout = time.perf_counter() - t_setup - t_gen
     n = lbm.n_sites
     lbm.SetInitialConditions()
+    # launch shape picked by the library's autotuner (its trial steps are warm-up)
+    variant, tuned_ms = lbm.autotune(3)
     lbm.DoTimeStep(args.warmup)
     # ---- device-resident timed region ---------------------------------------
     sampler = ClockSampler()
@@ -313,15 +315,16 @@ def main():
                 "algorithmic_bytes_per_launch": B_ALG[prec] * n,
                 "kernel": "hlbg::k_stream_collide<%d>" % prec, "launch_ms": per_launch}
     # ---- end to end through the C ABI: per step, H2D of that step's iolet values,
-    # the update, the StabilityTester/convergence reduction and its D2H read-back
+    # the update with the StabilityTester fused into it, and the D2H read-back of
+    # its stats (stability, mass, max |du| for the convergence test), synchronous
     st = capi.Stats()
     ke = max(1, min(args.e2e_steps, args.steps))
+    capi.check(lbm._lib.hlbg_step_monitored(lbm.ctx, 1, C.byref(st)), lbm.ctx)  # records velocities
     barrier(dist)
     lbm._lib.hlbg_sync(lbm.ctx)
     t0 = time.perf_counter()
     for _ in range(ke):
-        capi.check(lbm._lib.hlbg_step(lbm.ctx, 1, None), lbm.ctx)
-        rc = lbm._lib.hlbg_reduce(lbm.ctx, C.byref(st))
+        rc = lbm._lib.hlbg_step_monitored(lbm.ctx, 1, C.byref(st))
         if rc not in (0, capi.HLBG_ERR_UNSTABLE):
             capi.check(rc, lbm.ctx)
     dt = time.perf_counter() - t0
@@ -329,9 +332,10 @@ def main():
     dt = max_over_ranks(dist, dt)
     n_io = len(case.inlets) + len(case.outlets)
     e2e = {"value": WORLD * n * ke / dt / 1e6, "unit": "MLUPS", "steps": ke,
-           "h2d_bytes_per_step": 2 * 8 * n_io, "d2h_bytes_per_step": 4 * 8,
-           "path": "hlbg_step(1) + hlbg_reduce per step (iolet values in, stability/convergence out)"}
-    stable = st.unstable_sites == 0
+           "h2d_bytes_per_step": 2 * 8 * n_io, "d2h_bytes_per_step": 5 * 8,
+           "path": "hlbg_step_monitored(1) per step: iolet values in, update with the fused "
+                   "StabilityTester, its stats (mass, max |du|, min f, unstable count) out"}
+    stable = st.unstable_sites == 0 and st.time_step > 0
     # ---- CPU baseline ---------------------------------------------------------
     cpu = None
     if RANK == 0 and not args.no_cpu:
@@ -341,7 +345,7 @@ def main():
                "sample": "%d fluid sites (first Morton-ordered blocks of the same geometry), %d steps, "
                          "FP64 oracle, scalar order, OpenMP" % (cn, ck)}
     launches = args.steps * int(lbm._lib.hlbg_launches_per_step(lbm.ctx))
-    cfg.update({"fluid_sites": int(n), "slots": int(lbm.n_slots),
+    cfg.update({"fluid_sites": int(n), "slots": int(lbm.n_slots), "launch_variant": int(variant),
                 "collision_counts": list(lbm.collision_counts), "device_bytes": lbm.device_bytes(),
                 "l2": "inputs (distribution arrays) far larger than L2; no flush",
                 "setup_s": {"generate": round(t_gen, 2), "layout_upload": round(t_layout, 2)},

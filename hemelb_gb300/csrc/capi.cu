@@ -100,6 +100,9 @@ struct hlbg_ctx {
   int32_t* d_block_nbr = nullptr;
   int32_t* d_block_xyz = nullptr;
   uint32_t* d_site_code = nullptr;
+  uint16_t* d_slot2site = nullptr;  // packed blocks: local site of each slot
+  uint16_t* d_site2slot = nullptr;  // packed blocks: slot of each local site
+  std::vector<uint16_t> h_slot2site;
   uint8_t* d_block_bulk = nullptr;
   uint32_t* d_b_wall = nullptr;
   uint32_t* d_b_iolet = nullptr;
@@ -146,6 +149,15 @@ struct hlbg_ctx {
   double* d_steady = nullptr;
   long long* d_steady_n = nullptr;
   long long* h_steady_n = nullptr;  // pinned copy of the counters
+  // fused StabilityTester: per-slot velocity of the last monitored step, partials
+  // of the two reduction stages, the recorded-velocity flag and the last result
+  void* d_mon_u = nullptr;
+  double* d_mon_part = nullptr;
+  double* d_mon_part2 = nullptr;
+  int32_t* d_mon_state = nullptr;
+  double* d_mon_result = nullptr;
+  double* h_mon_result = nullptr;  // pinned
+  bool mon_recorded = false;       // host view: velocities of the current state recorded
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t dev_bytes = 0;
@@ -196,6 +208,8 @@ void fill_args(hlbg_ctx* ctx, StepArgs& a) {
   a.stride = ctx->nslot;
   a.nslot = ctx->nslot;
   a.block_nbr = ctx->d_block_nbr;
+  a.slot2site = ctx->d_slot2site;
+  a.site2slot = ctx->d_site2slot;
   a.site_code = ctx->d_site_code;
   a.block_bulk = ctx->d_block_bulk;
   a.b_wall = ctx->d_b_wall;
@@ -530,9 +544,42 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   ctx->n_ps = (int64_t)ctx->h_ps_slot.size();
   ctx->nb = nb;
   ctx->nslot = nslot;
+  // Pack every block that is not entirely fluid: its fluid sites take slots
+  // 0 .. nf-1 in site order and its solid sites the rest, so a partly fluid block
+  // moves whole 32-byte sectors instead of every z-row that touches fluid.
+  // Everything above was built with slot = site; map it now.
+  std::vector<uint16_t> site2slot((size_t)nslot), slot2site((size_t)nslot);
+  std::vector<uint8_t> packed((size_t)nb, 0);
+  parallel_for(nb, [&](int64_t b) {
+    int nf = 0;
+    for (int w = 0; w < 8; ++w) nf += __builtin_popcountll(mask[b * 8 + w]);
+    packed[b] = nf < 512;
+    int j = 0;
+    for (int want = 1; want >= 0; --want)  // fluid sites first, then solid ones
+      for (int l = 0; l < 512; ++l) {
+        if ((fluid(b * 512 + l) != 0) != (want == 1)) continue;
+        site2slot[b * 512 + l] = (uint16_t)j;
+        slot2site[b * 512 + j] = (uint16_t)l;
+        ++j;
+      }
+  });
+  auto slot_of = [&](int64_t site) { return (site & ~(int64_t)511) | site2slot[site]; };
+  {
+    std::vector<uint32_t> pc((size_t)nslot, 0);
+    for (int64_t t = 0; t < nslot; ++t) pc[slot_of(t)] = code[t];
+    code.swap(pc);
+  }
+  for (auto& v : ctx->h_rec_slot) v = (int32_t)slot_of(v);
+  for (auto& v : ctx->h_ref2slot) v = (int32_t)slot_of(v);
+  for (auto& v : ctx->h_ps_slot) v = (int32_t)slot_of(v);
+  for (auto& e : bnbr)
+    if (e >= 0 && packed[e]) e |= kPackedBit;
+  ctx->h_slot2site = slot2site;
   // device copies
   int rc;
   if ((rc = upload(ctx, &ctx->d_block_nbr, bnbr))) return rc;
+  if ((rc = upload(ctx, &ctx->d_slot2site, slot2site))) return rc;
+  if ((rc = upload(ctx, &ctx->d_site2slot, site2slot))) return rc;
   if ((rc = upload(ctx, &ctx->d_block_xyz, ctx->h_block_xyz))) return rc;
   if ((rc = upload(ctx, &ctx->d_site_code, code))) return rc;
   if ((rc = upload(ctx, &ctx->d_block_bulk, bulk))) return rc;
@@ -558,6 +605,66 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   if ((rc = upload(ctx, &ctx->d_ps_slot, ctx->h_ps_slot))) return rc;
   if ((rc = upload(ctx, &ctx->d_ps_dir, ctx->h_ps_dir))) return rc;
   if ((rc = upload(ctx, &ctx->d_ps_q, ctx->h_ps_q))) return rc;
+  return HLBG_OK;
+}
+
+constexpr int64_t kMonStage2 = 1024;
+
+// Buffers of the fused StabilityTester, allocated on first use.
+int mon_prepare(hlbg_ctx* ctx) {
+  if (ctx->d_mon_u) return HLBG_OK;
+  const size_t es = ctx->prec == 0 ? sizeof(double) : sizeof(float);
+  uint8_t* u = nullptr;
+  int rc = dev_alloc(ctx, &u, 3 * (size_t)ctx->nslot * es);
+  if (rc) return rc;
+  ctx->d_mon_u = u;
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_part, 4 * (size_t)(ctx->nslot / 128)))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_part2, 4 * (size_t)kMonStage2))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_state, 1))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_result, 5))) return rc;
+  CK(cudaMallocHost((void**)&ctx->h_mon_result, 5 * sizeof(double)));
+  CK(cudaMemsetAsync(ctx->d_mon_state, 0, sizeof(int32_t), ctx->stream));
+  ctx->mon_recorded = false;
+  return HLBG_OK;
+}
+
+// The distributions changed outside a monitored step: the recorded velocities no
+// longer belong to the state, so the next monitored step only records.
+int mon_invalidate(hlbg_ctx* ctx) {
+  if (ctx->d_mon_state && ctx->mon_recorded) {
+    CK(cudaMemsetAsync(ctx->d_mon_state, 0, sizeof(int32_t), ctx->stream));
+    ctx->mon_recorded = false;
+  }
+  return HLBG_OK;
+}
+
+int64_t monitored_grid(const hlbg_ctx* ctx) {
+  switch (ctx->prec) {
+    case 0: return monitored_grid_0(ctx->nslot, ctx->sc_variant);
+    case 1: return monitored_grid_1(ctx->nslot, ctx->sc_variant);
+    default: return monitored_grid_2(ctx->nslot, ctx->sc_variant);
+  }
+}
+
+// Monitor fields of a step's arguments (the kernel then records velocities and
+// writes one partial per CTA).
+void mon_args(hlbg_ctx* ctx, StepArgs& a) {
+  a.mon_u = ctx->d_mon_u;
+  a.mon_part = ctx->d_mon_part;
+  a.mon_nparts = monitored_grid(ctx);
+  a.mon_state = ctx->d_mon_state;
+}
+
+// The two reduction stages after a monitored step (steady: count the check).
+int mon_reduce(hlbg_ctx* ctx, const StepArgs& a, bool steady, cudaStream_t st) {
+  const int64_t n2 = std::min<int64_t>(kMonStage2, a.mon_nparts);
+  SteadyArgs sa{ctx->d_steady, ctx->d_steady ? ctx->d_steady + 1 : nullptr, ctx->d_steady_n};
+  switch (ctx->prec) {
+    case 0: launch_mon_reduce_0(a.mon_part, a.mon_nparts, ctx->d_mon_part2, n2, ctx->d_mon_state, ctx->d_mon_result, sa, steady, st); break;
+    case 1: launch_mon_reduce_1(a.mon_part, a.mon_nparts, ctx->d_mon_part2, n2, ctx->d_mon_state, ctx->d_mon_result, sa, steady, st); break;
+    default: launch_mon_reduce_2(a.mon_part, a.mon_nparts, ctx->d_mon_part2, n2, ctx->d_mon_state, ctx->d_mon_result, sa, steady, st); break;
+  }
+  CK(cudaGetLastError());
   return HLBG_OK;
 }
 
@@ -597,6 +704,10 @@ int graph_steps(hlbg_ctx* ctx, int n, bool check) {
         }
     }
   }
+  if (!check) {
+    int rc = mon_invalidate(ctx);
+    if (rc) return rc;
+  }
   hlbg_ctx::GraphKey key{n, ctx->cur, check ? 1 : 0};
   auto it = ctx->graphs.find(key);
   if (it == ctx->graphs.end()) {
@@ -609,36 +720,16 @@ int graph_steps(hlbg_ctx* ctx, int n, bool check) {
       if (e != cudaSuccess) rc = fail(ctx, HLBG_ERR_CUDA, cudaGetErrorString(e));
     }
     const int cur0 = ctx->cur;
-    const int64_t nparts = (ctx->nslot + 255) / 256;
     StepArgs a;
     for (int k = 0; k < n && !rc; ++k) {
       fill_args(ctx, a);
       a.iolet_rho = ctx->d_io_tab + (size_t)k * 2 * ctx->n_io;
       a.iolet_umax = a.iolet_rho + ctx->n_io;
+      if (check) mon_args(ctx, a);
       rc = launch_collide(ctx, a, ctx->stream);
       if (!rc) rc = run_post(ctx, ctx->stream, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps);
       ctx->cur ^= 1;
-      if (!rc && check) {
-        MonitorArgs ma{};
-        ma.f_cur = ctx->f[ctx->cur];
-        ma.f_prev = ctx->f[ctx->cur ^ 1];
-        ma.stride = ctx->nslot;
-        ma.nslot = ctx->nslot;
-        ma.site_code = ctx->d_site_code;
-        ma.block_bulk = ctx->d_block_bulk;
-        ma.part_mass = ctx->d_part;
-        ma.part_max = ctx->d_part + nparts;
-        ma.part_min = ctx->d_part + 2 * nparts;
-        ma.part_bad = ctx->d_part_bad;
-        ma.fp16_scale = ctx->fp16_scale;
-        ma.fp16_inv_scale = 1.0f / ctx->fp16_scale;
-        SteadyArgs sa{ctx->d_steady, ctx->d_steady + 1, ctx->d_steady_n};
-        switch (ctx->prec) {
-          case 0: launch_steady_check_0(ma, sa, ctx->stream); break;
-          case 1: launch_steady_check_1(ma, sa, ctx->stream); break;
-          default: launch_steady_check_2(ma, sa, ctx->stream); break;
-        }
-      }
+      if (!rc && check) rc = mon_reduce(ctx, a, true, ctx->stream);
     }
     ctx->cur = cur0;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
@@ -657,6 +748,7 @@ int graph_steps(hlbg_ctx* ctx, int n, bool check) {
   if (ctx->n_io) CK(cudaEventRecord(ctx->io_copied, ctx->stream));
   ctx->cur ^= (n & 1);
   ctx->t1 += n;
+  if (check) ctx->mon_recorded = true;
   return HLBG_OK;
 }
 
@@ -677,13 +769,15 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_ps_slot,   ctx->d_ps_dir,    ctx->d_ps_q,      ctx->d_iolets,
                   ctx->d_io_tab,    ctx->d_stage,     ctx->d_stage_rho, ctx->d_stage_u,
                   ctx->d_list,      ctx->d_part,      ctx->d_part_bad,  ctx->d_steady,
-                  ctx->d_steady_n};
+                  ctx->d_steady_n,  ctx->d_slot2site, ctx->d_site2slot, ctx->d_mon_u,
+                  ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
   if (ctx->d_blk_omega) cudaFree(ctx->d_blk_omega);
   if (ctx->h_io_tab) cudaFreeHost(ctx->h_io_tab);
   if (ctx->h_steady_n) cudaFreeHost(ctx->h_steady_n);
+  if (ctx->h_mon_result) cudaFreeHost(ctx->h_mon_result);
   if (ctx->io_copied) cudaEventDestroy(ctx->io_copied);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -799,7 +893,7 @@ int hlbg_site_coords(const hlbg_ctx* ctx, int32_t* xyz) {
   if (!ctx || !xyz) return HLBG_ERR_INVAL;
   for (int64_t i = 0; i < ctx->nsites; ++i) {
     const int64_t s = ctx->h_ref2slot[i], b = s >> 9;
-    const int l = (int)(s & 511);
+    const int l = ctx->h_slot2site[s];
     xyz[3 * i] = ctx->h_block_xyz[3 * b] * 8 + (l >> 6);
     xyz[3 * i + 1] = ctx->h_block_xyz[3 * b + 1] * 8 + ((l >> 3) & 7);
     xyz[3 * i + 2] = ctx->h_block_xyz[3 * b + 2] * 8 + (l & 7);
@@ -808,6 +902,10 @@ int hlbg_site_coords(const hlbg_ctx* ctx, int32_t* xyz) {
 }
 
 int hlbg_init_equilibrium(hlbg_ctx* ctx, double density, double vx, double vy, double vz) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx) return HLBG_ERR_INVAL;
   if (!(density > 0.0)) return fail(ctx, HLBG_ERR_INVAL, "density must be positive");
   // EquilibriumInitialCondition::SetFs (Code/lb/InitialCondition.hpp:40-52):
@@ -845,6 +943,10 @@ int hlbg_init_equilibrium(hlbg_ctx* ctx, double density, double vx, double vy, d
 }
 
 int hlbg_init_equilibrium_field(hlbg_ctx* ctx, const double* rho, const double* u) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx || !rho || !u) return HLBG_ERR_INVAL;
   int rc = ensure_stage(ctx);
   if (rc) return rc;
@@ -880,6 +982,10 @@ int hlbg_init_equilibrium_field(hlbg_ctx* ctx, const double* rho, const double* 
 }
 
 int hlbg_step(hlbg_ctx* ctx, int32_t nsteps, void* cuda_stream) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx || nsteps < 0) return HLBG_ERR_INVAL;
   if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
   cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
@@ -942,19 +1048,18 @@ int hlbg_run_to_steady(hlbg_ctx* ctx, double tol, double u_ref, int64_t max_step
                        int64_t* steps_to_steady, int64_t* steps_run, double* final_rel_du) {
   // Time steps until StabilityTester's convergence test holds: after every step,
   // max over sites |u_new - u_old| / U_ref <= tol (Code/lb/StabilityTester.h:91-183),
-  // evaluated on the device.  Steps run in CUDA graphs of check_batch steps, each
-  // step followed by its check; the host reads the device counters after each
-  // batch, so up to check_batch - 1 steps run past the first converged one.
+  // evaluated on the device by the fused monitor (the check of step k is made
+  // while step k + 1 collides).  Steps run in CUDA graphs of check_batch steps;
+  // the host reads the device counters after each batch, so between 1 and
+  // check_batch steps run past the first converged one.
   if (!ctx || !(tol > 0.0) || !(u_ref > 0.0) || max_steps < 1 || check_batch < 1 ||
       check_batch > kStepBatch)
     return HLBG_ERR_INVAL;
   if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
-  const int64_t nparts = (ctx->nslot + 255) / 256;
-  if (!ctx->d_part) {
-    int rc = dev_alloc(ctx, &ctx->d_part, (size_t)nparts * 3);
-    if (!rc) rc = dev_alloc(ctx, &ctx->d_part_bad, (size_t)nparts);
-    if (rc) return rc;
-  }
+  int rc0 = mon_prepare(ctx);
+  if (rc0) return rc0;
+  // every call starts by recording velocities: its first check is its first step
+  CK(cudaMemsetAsync(ctx->d_mon_state, 0, sizeof(int32_t), ctx->stream));
   if (!ctx->d_steady) {
     int rc = dev_alloc(ctx, &ctx->d_steady, 2);
     if (!rc) rc = dev_alloc(ctx, &ctx->d_steady_n, 3);
@@ -994,9 +1099,51 @@ int hlbg_run_to_steady(hlbg_ctx* ctx, double tol, double u_ref, int64_t max_step
   return HLBG_OK;
 }
 
+int hlbg_step_monitored(hlbg_ctx* ctx, int32_t nsteps, hlbg_stats* out) {
+  // nsteps time steps with the StabilityTester fused into the update; the stats
+  // are those of the check made during the last step, i.e. of the step before it.
+  if (!ctx || nsteps < 1 || !out) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  int rc = mon_prepare(ctx);
+  if (rc) return rc;
+  cudaStream_t st = ctx->stream;
+  StepArgs a;
+  for (int done = 0; done < nsteps;) {
+    const int n = std::min(kStepBatch, nsteps - done);
+    if ((rc = upload_iolet_table(ctx, n, st))) return rc;
+    for (int k = 0; k < n; ++k) {
+      fill_args(ctx, a);
+      a.iolet_rho = ctx->d_io_tab + (size_t)k * 2 * ctx->n_io;
+      a.iolet_umax = a.iolet_rho + ctx->n_io;
+      mon_args(ctx, a);
+      if ((rc = launch_collide(ctx, a, st))) return rc;
+      if ((rc = run_post(ctx, st, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps))) return rc;
+      ctx->cur ^= 1;
+      ctx->t1++;
+      if ((rc = mon_reduce(ctx, a, false, st))) return rc;
+      ctx->mon_recorded = true;
+    }
+    done += n;
+  }
+  CK(cudaMemcpyAsync(ctx->h_mon_result, ctx->d_mon_result, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const double* r = ctx->h_mon_result;
+  const bool valid = r[4] != 0.0;
+  out->mass = valid ? r[0] : 0.0;
+  out->max_du = valid ? r[1] : 0.0;
+  out->min_f = valid ? r[2] : 0.0;
+  out->unstable_sites = valid ? (int64_t)r[3] : 0;
+  out->time_step = valid ? (int64_t)ctx->t1 - 1 : -1;
+  return valid && r[3] > 0.0 ? HLBG_ERR_UNSTABLE : HLBG_OK;
+}
+
 int hlbg_average_time_levels(hlbg_ctx* ctx) {
   if (!ctx) return HLBG_ERR_INVAL;
   if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  {
+    int rc = mon_invalidate(ctx);
+    if (rc) return rc;
+  }
   AverageArgs aa{};
   aa.f_cur = ctx->f[ctx->cur];
   aa.f_prev = ctx->f[ctx->cur ^ 1];
@@ -1048,6 +1195,10 @@ int hlbg_sync(hlbg_ctx* ctx) {
 }
 
 int hlbg_stream_and_collide_range(hlbg_ctx* ctx, int64_t first, int64_t count) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx || first < 0 || count < 0 || first + count > ctx->nsites) return HLBG_ERR_INVAL;
   if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
   if (count == 0) return HLBG_OK;
@@ -1068,6 +1219,10 @@ int hlbg_stream_and_collide_range(hlbg_ctx* ctx, int64_t first, int64_t count) {
 }
 
 int hlbg_post_step_range(hlbg_ctx* ctx, int64_t first, int64_t count) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx || first < 0 || count < 0 || first + count > ctx->nsites) return HLBG_ERR_INVAL;
   if (ctx->params.wall != HLBG_WALL_BFL || count == 0 || ctx->n_ps == 0) return HLBG_OK;
   // the PostStep links whose site lies in the contiguous-id range
@@ -1101,6 +1256,10 @@ int hlbg_post_step_range(hlbg_ctx* ctx, int64_t first, int64_t count) {
 }
 
 int hlbg_swap(hlbg_ctx* ctx) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx) return HLBG_ERR_INVAL;
   ctx->cur ^= 1;
   ctx->t1++;
@@ -1142,6 +1301,10 @@ static int gather_common(hlbg_ctx* ctx, double* out, int32_t which, bool to_host
 }
 
 static int scatter_common(hlbg_ctx* ctx, const double* in, int32_t which, bool from_host) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx || !in || (which != 0 && which != 1)) return HLBG_ERR_INVAL;
   int rc = ensure_stage(ctx);
   if (rc) return rc;
@@ -1344,6 +1507,10 @@ int hlbg_iolet_density(const hlbg_ctx* ctx, int32_t is_outlet, int32_t index, ui
 }
 
 int hlbg_time_kernels(hlbg_ctx* ctx, int32_t nsteps, float* collide_ms, float* post_ms) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   // Same work as hlbg_step, with CUDA events recorded on the context stream
   // around every launch; returns the summed device time of each kernel kind.
   if (!ctx || !collide_ms || !post_ms || nsteps < 0) return HLBG_ERR_INVAL;
@@ -1385,6 +1552,10 @@ int hlbg_time_kernels(hlbg_ctx* ctx, int32_t nsteps, float* collide_ms, float* p
 }
 
 int hlbg_time_steps(hlbg_ctx* ctx, int32_t nsteps, float* ms) {
+  if (ctx) {  // the distributions change outside a monitored step
+    const int rc_ = mon_invalidate(ctx);
+    if (rc_) return rc_;
+  }
   if (!ctx || !ms) return HLBG_ERR_INVAL;
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));

@@ -1,14 +1,19 @@
 // Device kernels of the GB300 lattice-Boltzmann update (D3Q19).
 //
-// Layout in HBM (built by layout.cpp):
-//   * non-empty 8^3 blocks in Morton order; slot = block * 512 + local index,
-//     local = (x * 8 + y) * 8 + z, the reference's SiteTraverser order;
+// Layout in HBM (built by the host in capi.cu, build_layout):
+//   * non-empty 8^3 blocks in z-column order (2-D Morton order of the block's
+//     (x, y), then z); local site index l = (x * 8 + y) * 8 + z, the reference's
+//     SiteTraverser order; slot = block * 512 + j;
+//   * a block that is entirely fluid keeps j = l; in every other block the fluid
+//     sites are packed into slots 0 .. nf-1 in site order and the solid sites
+//     follow, so the distributions of a partly fluid block fill whole 32-byte
+//     sectors; slot2site / site2slot translate for those blocks;
 //   * distributions block-major structure-of-arrays: for block b, direction d and
-//     local site l, f[(b * 19 + d) * 512 + l]; each block's 19 x 512 values are
+//     slot j, f[(b * 19 + d) * 512 + j]; each block's 19 x 512 values are
 //     contiguous, so a site's 19 loads share one base address; two copies
 //     (old / new) swapped every step (FieldData::SwapOldAndNew);
 //   * block_nbr[block * 27 + (dx+1)*9 + (dy+1)*3 + (dz+1)] = neighbouring block
-//     index or -1, staged in shared memory per CTA;
+//     index, with kPackedBit set when that block is packed, or -1;
 //   * site_code[slot] = 0 solid, 1 bulk (all 18 links fluid-fluid, no wall or
 //     iolet bit), 2 + r for boundary record r;
 //   * boundary records (wall / iolet masks, iolet id, collision type, cut
@@ -75,12 +80,25 @@ struct IoletDev {
   int32_t pad_;
 };
 
+// Flag of a block_nbr entry whose block has its fluid sites packed (slot != site).
+constexpr int32_t kPackedBit = 1 << 30;
+
 struct StepArgs {
   const void* f_old;
   void* f_new;
   int64_t stride;  // elements between directions (= slot count)
   int64_t nslot;
   const int32_t* block_nbr;
+  const uint16_t* slot2site;  // [nslot] local site of each slot (packed blocks)
+  const uint16_t* site2slot;  // [nslot] slot of each local site (packed blocks)
+  // Fused StabilityTester (monitored steps only): each site's velocity at its last
+  // update, u[(block * 3 + c) * 512 + slot] (double for FP64, float otherwise); the
+  // per-CTA partials [mass | max |du| | min f | unstable] with stride mon_nparts;
+  // mon_state 0 while no velocity has been recorded since the state was set.
+  void* mon_u;
+  double* mon_part;
+  int64_t mon_nparts;
+  const int32_t* mon_state;
   const uint32_t* site_code;
   const uint8_t* block_bulk;  // 1: all 512 slots are bulk sites
   const uint32_t* b_wall;

@@ -66,6 +66,34 @@ __device__ __noinline__ typename Calc<P>::T iolet_link_value(
   return fpost_d - (T)ladd_correction64(io, a.iolet_umax[gi], rho, gx, gy, gz, d);
 }
 
+// Entry k of the 27-block table around a site's block (neighbour block index,
+// kPackedBit when that block is packed, -1 when absent): served by shuffle from
+// lanes 0..26 in the all-slots kernel, from the global table in the list kernel.
+struct ShflBase {
+  int32_t reg;
+  __device__ __forceinline__ int32_t operator()(int k) const { return __shfl_sync(0xffffffffu, reg, k); }
+};
+struct GlobalBase {
+  const int32_t* tab;
+  __device__ __forceinline__ int32_t operator()(int k) const { return __ldg(tab + k); }
+};
+
+// Slot of local site tl in the block of table entry e (e >= 0).
+__device__ __forceinline__ int64_t target_slot(const StepArgs& a, int32_t e, int tl) {
+  const int64_t nb = e & ~kPackedBit;
+  const int ts = (e & kPackedBit) ? (int)__ldg(a.site2slot + (nb << 9) + tl) : tl;
+  return (nb << 9) + ts;
+}
+// Element offset of direction D of local site tl in the block of entry e (e >= 0).
+__device__ __forceinline__ int64_t target_off(const StepArgs& a, int32_t e, int D, int tl) {
+  const int64_t ts = target_slot(a, e, tl);
+  return fidx(ts, D);
+}
+// Local site index of slot s (its block's packed flag in `packed`).
+__device__ __forceinline__ int site_of_slot(const StepArgs& a, int64_t s, bool packed) {
+  return packed ? (int)__ldg(a.slot2site + s) : (int)(s & (kSites - 1));
+}
+
 // Per-link dispatch of a site next to a wall or an iolet, unrolled over the 19
 // directions (StreamerTypeFactory.h:65-79: iolet first, then wall, else bulk).
 template <int P, int D>
@@ -77,7 +105,7 @@ struct BoundaryAll {
                                              T mx, T my, T mz, const int32_t* block_xyz) {
     constexpr int inv = Lat::inv(D);
     const int64_t own = fidx(s, 0) - (int64_t)(s & (kSites - 1));  // this block's element base
-    const int l = (int)(s & (kSites - 1));
+    const int l = (int)(s & (kSites - 1));  // this site's slot in its block
     if (D > 0 && type >= 2 && ((im >> (D - 1)) & 1u)) {
       const bool is_inlet = (type == 2 || type == 4);
       const int gi = is_inlet ? ioid : a.n_in + ioid;
@@ -100,11 +128,11 @@ struct BoundaryAll {
       const int xx = x + cx, yy = y + cy, zz = z + cz;
       const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
       const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
-      const int64_t nbase = base(k);
-      if (nbase >= 0) {
-        const int64_t ns = nbase / Q + tl;  // neighbour slot (block * 512 + local)
+      const int32_t e = base(k);
+      if (e >= 0) {
+        const int64_t ns = target_slot(a, e, tl);
         const uint32_t nc = a.block_bulk[ns >> 9] ? 1u : a.site_code[ns];
-        if (nc != 0) Store<P>::store(fn + nbase, D * kSites + tl, fpost[D], a);
+        if (nc != 0) Store<P>::store(fn, fidx(ns, D), fpost[D], a);
       }
     }
     BoundaryAll<P, D + 1>::run(fn, a, base, s, x, y, z, wm, im, type, ioid, r, fpost, m0, mx, my, mz,
@@ -119,26 +147,6 @@ struct BoundaryAll<P, Q> {
                                              T, const int32_t*) {}
 };
 
-// Element offset (block * 19 * 512) of the 27 blocks around a site's block: from
-// shared memory in the all-slots kernel, from the global table in the list kernel.
-struct SmemBase {
-  const int64_t* sh;
-  __device__ __forceinline__ int64_t operator()(int k) const { return sh[k]; }
-};
-struct ShflBase {
-  int32_t reg;  // lane k < 27 holds neighbour block k
-  __device__ __forceinline__ int64_t operator()(int k) const {
-    return (int64_t)__shfl_sync(0xffffffffu, reg, k) * (Q * kSites);
-  }
-};
-struct GlobalBase {
-  const int32_t* tab;
-  __device__ __forceinline__ int64_t operator()(int k) const {
-    const int32_t nb = __ldg(tab + k);
-    return nb < 0 ? (int64_t)-1 : (int64_t)nb * (Q * kSites);
-  }
-};
-
 // Push of a bulk site's post-collision value along direction D (compile-time):
 // neighbour block from the 27-entry table, local index by wrap-around arithmetic.
 template <int P, int D>
@@ -150,7 +158,7 @@ struct PushAll {
     const int xx = x + cx, yy = y + cy, zz = z + cz;
     const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
     const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
-    Store<P>::store(fn + base(k), D * kSites + tl, fpost[D], a);
+    Store<P>::store(fn, target_off(a, base(k), D, tl), fpost[D], a);
     PushAll<P, D + 1>::run(fn, a, base, x, y, z, fpost);
   }
 };
@@ -171,8 +179,8 @@ struct PushBulk {
     const int xx = x + cx, yy = y + cy, zz = z + cz;
     const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
     const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
-    const int64_t nb = base(k);
-    if (store) Store<P>::store(fn + nb, D * kSites + tl, fpost[D], a);
+    const int32_t e = base(k);  // every lane shuffles
+    if (store) Store<P>::store(fn, target_off(a, e, D, tl), fpost[D], a);
     PushBulk<P, D + 1>::run(fn, a, base, x, y, z, store, fpost);
   }
 };
@@ -191,7 +199,7 @@ template <int P, int D>
 struct PushMixed {
   template <class S, class T, class B>
   static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, int x, int y,
-                                             int z, int l, int64_t own, bool active, bool row_fluid,
+                                             int z, int j, int64_t own, bool active, bool row_fluid,
                                              uint64_t links,
                                              int64_t r, int type, int ioid, const T* fpost, T m0,
                                              T mx, T my, T mz, int64_t b,
@@ -201,23 +209,25 @@ struct PushMixed {
     const int xx = x + cx, yy = y + cy, zz = z + cz;
     const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
     const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
-    const int64_t nb = base(k);
+    const int32_t e = base(k);  // every lane shuffles
     const unsigned lc = (unsigned)((links >> (3 * D)) & 7u);
-    int64_t off = nb + D * kSites + tl;
+    int64_t off = 0;
     T v = fpost[D];
     bool st = true;
     if (!active) {
       // A solid slot is never written by a push nor ever read; a zero there completes
-      // the 32-byte sectors of its row when the row also holds fluid sites (rows
-      // without any receive no write at all and stay untouched).
-      off = own + D * kSites + l;
+      // the 32-byte sector of slots it shares with fluid slots (sectors without any
+      // receive no write at all and stay untouched).
+      off = own + D * kSites + j;
       v = (T)0;
       st = row_fluid;
-    } else if (lc != HLBG_LC_PUSH) {
+    } else if (lc == HLBG_LC_PUSH) {
+      off = target_off(a, e, D, tl);
+    } else {
       if (lc == HLBG_LC_SKIP) {
         st = false;
       } else {
-        off = own + inv * kSites + l;
+        off = own + inv * kSites + j;
         if (lc == HLBG_LC_BFL) {
           const T q = (T)a.b_cut[r * (Q - 1) + D - 1];
           v = (fpost[D] + ((T)2.0 * q - (T)1) * fpost[inv]) / ((T)2.0 * q);
@@ -226,7 +236,7 @@ struct PushMixed {
       }
     }
     if (st) Store<P>::store(fn, off, v, a);
-    PushMixed<P, D + 1>::run(fn, a, base, x, y, z, l, own, active, row_fluid, links, r, type, ioid,
+    PushMixed<P, D + 1>::run(fn, a, base, x, y, z, j, own, active, row_fluid, links, r, type, ioid,
                              fpost, m0, mx, my, mz, b, block_xyz);
   }
 };
@@ -238,6 +248,103 @@ struct PushMixed<P, Q> {
                                              const T*, T, T, T, T, int64_t, const int32_t*) {}
 };
 
+// StabilityTester::PostSendToParent (Code/lb/StabilityTester.h:91-149) and
+// ComputeRelativeDifference (:160-183) plus total mass: one slot per thread, one
+// partial per CTA, reduced by k_monitor_final in a fixed order (deterministic).
+struct MonAcc {
+  double mass, maxdu, minf;
+  unsigned long long bad;
+};
+
+__device__ __forceinline__ void mon_combine(MonAcc& a, const MonAcc& b) {
+  a.mass += b.mass;
+  if (!(b.maxdu <= a.maxdu)) a.maxdu = b.maxdu;  // NaN-propagating max
+  a.minf = fmin(a.minf, b.minf);
+  a.bad += b.bad;
+}
+
+__device__ __forceinline__ MonAcc mon_shfl(const MonAcc& v, int off) {
+  MonAcc o;
+  o.mass = __shfl_down_sync(0xffffffffu, v.mass, off);
+  o.maxdu = __shfl_down_sync(0xffffffffu, v.maxdu, off);
+  o.minf = __shfl_down_sync(0xffffffffu, v.minf, off);
+  o.bad = __shfl_down_sync(0xffffffffu, v.bad, off);
+  return o;
+}
+
+// CTA-wide reduction (up to 1024 threads) in a fixed order; result valid in thread 0.
+__device__ __forceinline__ MonAcc mon_block(MonAcc v) {
+  __shared__ MonAcc sh[32];
+  for (int off = 16; off > 0; off >>= 1) mon_combine(v, mon_shfl(v, off));
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : MonAcc{0.0, 0.0, 1.0e300, 0ull};
+    for (int off = 16; off > 0; off >>= 1) mon_combine(v, mon_shfl(v, off));
+  }
+  return v;
+}
+
+// Fused StabilityTester for one fluid site of a monitored step
+// (Code/lb/StabilityTester.h:91-183): the velocity of the state being collided,
+// m / rho with the moments of the collision (the reference's
+// CalculateDensityAndMomentum), against the one recorded when this site was last
+// updated; f > 0 over all directions; the density for the mass.  The new velocity
+// is recorded for the next step.
+template <int P>
+__device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const typename Calc<P>::T* f,
+                                         typename Calc<P>::T m0, typename Calc<P>::T mx,
+                                         typename Calc<P>::T my, typename Calc<P>::T mz, MonAcc& acc,
+                                         bool check) {
+  const int64_t ui = (s >> 9) * (3 * kSites) + (s & (kSites - 1));
+  if constexpr (P == 0) {
+    double* u = static_cast<double*>(a.mon_u);
+    const double ux = mx / m0, uy = my / m0, uz = mz / m0;
+    if (check) {
+      const double dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
+      const double du = sqrt(dot3d(dx, dy, dz, dx, dy, dz));
+      if (!(du <= acc.maxdu)) acc.maxdu = du;
+      acc.mass += m0;
+      bool bad = false;
+      double mn = f[0];
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        bad |= !(f[d] > 0.0);
+        mn = fmin(mn, f[d]);
+      }
+      acc.minf = fmin(acc.minf, mn);
+      acc.bad += bad ? 1ull : 0ull;
+    }
+    u[ui] = ux;
+    u[ui + kSites] = uy;
+    u[ui + 2 * kSites] = uz;
+  } else {
+    float* u = static_cast<float*>(a.mon_u);
+    const float ir = 1.f / (1.f + m0);
+    const float ux = mx * ir, uy = my * ir, uz = mz * ir;
+    if (check) {
+      const float dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
+      const double du = (double)sqrtf(dx * dx + dy * dy + dz * dz);
+      if (!(du <= acc.maxdu)) acc.maxdu = du;
+      acc.mass += 1.0 + (double)m0;
+      bool bad = false;
+      float mn = 1.0e30f;
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        const float fv = f[d] + weight_f(d);
+        bad |= !(fv > 0.f);
+        mn = fminf(mn, fv);
+      }
+      acc.minf = fmin(acc.minf, (double)mn);
+      acc.bad += bad ? 1ull : 0ull;
+    }
+    u[ui] = ux;
+    u[ui + kSites] = uy;
+    u[ui + 2 * kSites] = uz;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // One site: collide, then push along the 19 links.
 // ---------------------------------------------------------------------------
@@ -248,9 +355,10 @@ __device__ __forceinline__ void site_update(const StepArgs& a, const B& base,
   using St = Store<P>;
   using S = typename St::S;
   using T = typename Calc<P>::T;
-  const int l = (int)(s & (kSites - 1));
+  const int j = (int)(s & (kSites - 1));
   const int64_t b = s >> 9;
-  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + l;
+  const int l = site_of_slot(a, s, (__ldg(tab + 13) & kPackedBit) != 0);
+  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + j;
   S* fn = static_cast<S*>(a.f_new);
   T f[Q], fpost[Q];
 #pragma unroll
@@ -269,9 +377,10 @@ __device__ __forceinline__ void site_update(const StepArgs& a, const B& base,
 // One warp's 32 slots of one block (a warp never spans two blocks).  Lanes 0..26
 // hold the block's neighbour table and serve it to the bulk pushes by shuffle, so
 // every lane of a warp with any fluid site stays converged through the pushes.
-template <int P>
+template <int P, bool MON>
 __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
-                                             const int32_t* __restrict__ block_xyz) {
+                                             const int32_t* __restrict__ block_xyz, MonAcc& acc,
+                                             bool check) {
   using St = Store<P>;
   using S = typename St::S;
   using T = typename Calc<P>::T;
@@ -282,10 +391,12 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
   const uint32_t code = a.block_bulk[b] ? 1u : a.site_code[s];
   const unsigned fluid_lanes = __ballot_sync(0xffffffffu, code != 0);
   if (fluid_lanes == 0) return;
-  // lanes 8r..8r+7 hold one z-row (a 32-byte sector of each direction in FP32)
+  // lanes 8r..8r+7 hold eight consecutive slots (a 32-byte sector of each direction in FP32)
   const bool row_fluid = ((fluid_lanes >> (lane & ~7)) & 0xFFu) != 0;
-  const int l = (int)(s & (kSites - 1));
-  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + l;
+  const int j = (int)(s & (kSites - 1));
+  const bool packed = (__shfl_sync(0xffffffffu, tabreg, 13) & kPackedBit) != 0;
+  const int l = site_of_slot(a, s, packed);
+  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + j;
   S* fn = static_cast<S*>(a.f_new);
   T f[Q], fpost[Q];
   if (code != 0) {
@@ -297,6 +408,9 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
   }
   T m0, mx, my, mz;
   collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
+  if constexpr (MON) {
+    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check);
+  }
   const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
   const bool bnd = code >= 2;
   if (__ballot_sync(0xffffffffu, bnd) == 0) {
@@ -306,7 +420,7 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
     const uint64_t links = bnd ? a.b_links[r] : 0ull;
     const int type = bnd ? (int)a.b_type[r] : 0;
     const int ioid = bnd ? a.b_ioid[r] : 0;
-    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, l, b * (Q * kSites), code != 0, row_fluid,
+    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, j, b * (Q * kSites), code != 0, row_fluid,
                          links, r, type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
   }
 }
@@ -314,15 +428,77 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
 // All slots.  THREADS threads per CTA with at least MINB CTAs resident per SM;
 // PERSIST: a grid of resident CTAs striding over 128-slot chunks in order, else
 // one thread per slot.  The variants are the autotuner's candidates.
-template <int P, int THREADS, int MINB, bool PERSIST>
+template <int P, int THREADS, int MINB, bool PERSIST, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_stream_collide(StepArgs a, const int32_t* block_xyz) {
+  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  bool check = false;
+  if constexpr (MON) check = *a.mon_state != 0;
   if constexpr (!PERSIST) {
-    collide_slot<P>(a, (int64_t)blockIdx.x * THREADS + threadIdx.x, block_xyz);  // 512 | nslot
+    collide_slot<P, MON>(a, (int64_t)blockIdx.x * THREADS + threadIdx.x, block_xyz, acc, check);
   } else {
     const int64_t nchunk = a.nslot / THREADS;
     for (int64_t c = blockIdx.x; c < nchunk; c += gridDim.x)
-      collide_slot<P>(a, c * THREADS + threadIdx.x, block_xyz);
+      collide_slot<P, MON>(a, c * THREADS + threadIdx.x, block_xyz, acc, check);
+  }
+  if constexpr (MON) {
+    acc = mon_block(acc);
+    if (threadIdx.x == 0) {
+      const int64_t n = a.mon_nparts;
+      a.mon_part[blockIdx.x] = acc.mass;
+      a.mon_part[n + blockIdx.x] = acc.maxdu;
+      a.mon_part[2 * n + blockIdx.x] = acc.minf;
+      a.mon_part[3 * n + blockIdx.x] = (double)acc.bad;
+    }
+  }
+}
+
+// Second stage of the fused StabilityTester's reduction: CTA c folds partials
+// [c * per, (c + 1) * per) in a fixed order into out[c] (same layout, stride n_out).
+static __global__ void __launch_bounds__(256) k_mon_stage2(const double* __restrict__ in, int64_t n_in,
+                                                           int64_t per, double* __restrict__ out,
+                                                           int64_t n_out) {
+  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  const int64_t lo = (int64_t)blockIdx.x * per, hi = lo + per < n_in ? lo + per : n_in;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+    mon_combine(acc, MonAcc{in[i], in[n_in + i], in[2 * n_in + i], (unsigned long long)in[3 * n_in + i]});
+  __syncthreads();
+  acc = mon_block(acc);
+  if (threadIdx.x == 0) {
+    out[blockIdx.x] = acc.mass;
+    out[n_out + blockIdx.x] = acc.maxdu;
+    out[2 * n_out + blockIdx.x] = acc.minf;
+    out[3 * n_out + blockIdx.x] = (double)acc.bad;
+  }
+}
+
+// Last stage: result = [mass, max |du|, min f, unstable, valid]; valid is 0 for the
+// first step after the state was set (it only recorded velocities).  With sa, a
+// valid check is also counted for steady-state detection.
+// Every step then marks the recorded velocities as present.
+static __global__ void __launch_bounds__(256) k_mon_final(const double* __restrict__ part, int64_t n,
+                                                          int32_t* mon_state, double* result,
+                                                          SteadyArgs sa, int steady) {
+  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+    mon_combine(acc, MonAcc{part[i], part[n + i], part[2 * n + i], (unsigned long long)part[3 * n + i]});
+  __syncthreads();
+  acc = mon_block(acc);
+  if (threadIdx.x == 0) {
+    const int valid = *mon_state != 0;
+    result[0] = acc.mass;
+    result[1] = acc.maxdu;
+    result[2] = acc.minf;
+    result[3] = (double)acc.bad;
+    result[4] = valid;
+    if (steady && valid) {
+      const long long k = sa.counters[0] + 1;
+      sa.counters[0] = k;
+      *sa.last_du = acc.maxdu;
+      if (acc.bad && sa.counters[2] < 0) sa.counters[2] = k;
+      if (acc.maxdu <= *sa.threshold && sa.counters[1] < 0) sa.counters[1] = k;
+    }
+    *mon_state = 1;
   }
 }
 
@@ -368,8 +544,9 @@ __global__ void __launch_bounds__(128) k_iolet_links(StepArgs a, const int32_t* 
   const bool is_inlet = (type == 2 || type == 4);
   const int gi = is_inlet ? ioid : a.n_in + ioid;
   const int model = is_inlet ? a.inlet_model : a.outlet_model;
-  const int gx = block_xyz[3 * b] * 8 + (l >> 6), gy = block_xyz[3 * b + 1] * 8 + ((l >> 3) & 7),
-            gz = block_xyz[3 * b + 2] * 8 + (l & 7);
+  const int ls = site_of_slot(a, s, (__ldg(a.block_nbr + b * 27 + 13) & kPackedBit) != 0);
+  const int gx = block_xyz[3 * b] * 8 + (ls >> 6), gy = block_xyz[3 * b + 1] * 8 + ((ls >> 3) & 7),
+            gz = block_xyz[3 * b + 2] * 8 + (ls & 7);
 #pragma unroll 1
   for (int d = 1; d < Q; ++d) {
     if (((links >> (3 * d)) & 7u) != HLBG_LC_IOLET) continue;
@@ -547,44 +724,6 @@ __global__ void k_macro(GatherArgs ga) {
   }
 }
 
-// StabilityTester::PostSendToParent (Code/lb/StabilityTester.h:91-149) and
-// ComputeRelativeDifference (:160-183) plus total mass: one slot per thread, one
-// partial per CTA, reduced by k_monitor_final in a fixed order (deterministic).
-struct MonAcc {
-  double mass, maxdu, minf;
-  unsigned long long bad;
-};
-
-__device__ __forceinline__ void mon_combine(MonAcc& a, const MonAcc& b) {
-  a.mass += b.mass;
-  if (!(b.maxdu <= a.maxdu)) a.maxdu = b.maxdu;  // NaN-propagating max
-  a.minf = fmin(a.minf, b.minf);
-  a.bad += b.bad;
-}
-
-__device__ __forceinline__ MonAcc mon_shfl(const MonAcc& v, int off) {
-  MonAcc o;
-  o.mass = __shfl_down_sync(0xffffffffu, v.mass, off);
-  o.maxdu = __shfl_down_sync(0xffffffffu, v.maxdu, off);
-  o.minf = __shfl_down_sync(0xffffffffu, v.minf, off);
-  o.bad = __shfl_down_sync(0xffffffffu, v.bad, off);
-  return o;
-}
-
-// CTA-wide reduction (256 threads) in a fixed order; result valid in thread 0.
-__device__ __forceinline__ MonAcc mon_block(MonAcc v) {
-  __shared__ MonAcc sh[8];
-  for (int off = 16; off > 0; off >>= 1) mon_combine(v, mon_shfl(v, off));
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : MonAcc{0.0, 0.0, 1.0e300, 0ull};
-    for (int off = 4; off > 0; off >>= 1) mon_combine(v, mon_shfl(v, off));
-  }
-  return v;
-}
-
 template <int P>
 __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
   using St = Store<P>;
@@ -674,25 +813,6 @@ static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, in
   }
 }
 
-// Final reduction of the monitor partials for steady-state detection: one check
-// per call, counted on the device so that a captured graph of many steps (each
-// followed by its check) records the first converged step without host reads.
-static __global__ void __launch_bounds__(256) k_steady_final(MonitorArgs ma, int64_t nparts, SteadyArgs sa) {
-  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
-  for (int64_t i = threadIdx.x; i < nparts; i += blockDim.x)
-    mon_combine(acc, MonAcc{ma.part_mass[i], ma.part_max[i], ma.part_min[i], ma.part_bad[i]});
-  __syncthreads();
-  acc = mon_block(acc);
-  if (threadIdx.x == 0) {
-    const long long n = sa.counters[0] + 1;
-    sa.counters[0] = n;
-    *sa.last_du = acc.maxdu;
-    if (acc.bad && sa.counters[2] < 0) sa.counters[2] = n;
-    // a NaN maximum compares false and never counts as converged
-    if (acc.maxdu <= *sa.threshold && sa.counters[1] < 0) sa.counters[1] = n;
-  }
-}
-
 // Mean of the two time levels on every fluid slot (the arrays hold consecutive
 // states right after a step): removes the period-two component of the state.
 template <int P>
@@ -718,21 +838,21 @@ __global__ void __launch_bounds__(256) k_average(AverageArgs aa) {
 }  // namespace hlbg
 
 namespace hlbg {
-template <int P, int THREADS, int MINB, bool PERSIST>
+template <int P, int THREADS, int MINB, bool PERSIST, bool MON = false>
 void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
   unsigned g;
   if constexpr (PERSIST) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream_collide<P, THREADS, MINB, PERSIST>,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream_collide<P, THREADS, MINB, PERSIST, MON>,
                                                   THREADS, 0);
     const int64_t chunks = a.nslot / THREADS;
     g = (unsigned)std::min<int64_t>(chunks, (int64_t)sms * std::max(per_sm, 1));
   } else {
     g = (unsigned)(a.nslot / THREADS);
   }
-  if (g) k_stream_collide<P, THREADS, MINB, PERSIST><<<g, THREADS, 0, st>>>(a, bxyz);
+  if (g) k_stream_collide<P, THREADS, MINB, PERSIST, MON><<<g, THREADS, 0, st>>>(a, bxyz);
 }
 }  // namespace hlbg
 
@@ -746,6 +866,16 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       return;                                                                                   \
     }                                                                                           \
     if (P == 0) variant = -1;                                                                   \
+    if (a.mon_u) { /* one partial per CTA: the persistent shape is not used */                  \
+      switch (variant) {                                                                        \
+        case 1: launch_sc<P, 128, (P == 0 ? 2 : 8), false, true>(a, bxyz, st); break;           \
+        case 2: launch_sc<P, 256, (P == 0 ? 2 : 4), false, true>(a, bxyz, st); break;           \
+        case 3: launch_sc<P, 512, (P == 0 ? 1 : 2), false, true>(a, bxyz, st); break;           \
+        case -1: launch_sc<P, 128, 2, false, true>(a, bxyz, st); break;                         \
+        default: launch_sc<P, HLBG_SC_THREADS, HLBG_SC_MINB, false, true>(a, bxyz, st); break;  \
+      }                                                                                         \
+      return;                                                                                   \
+    }                                                                                           \
     switch (variant) {                                                                          \
       case 1: launch_sc<P, 128, (P == 0 ? 2 : 8), false>(a, bxyz, st); break;                   \
       case 2: launch_sc<P, 256, (P == 0 ? 2 : 4), false>(a, bxyz, st); break;                   \
@@ -754,6 +884,22 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       case -1: launch_sc<P, 128, 2, false>(a, bxyz, st); break;                                 \
       default: launch_sc<P, HLBG_SC_THREADS, HLBG_SC_MINB, false>(a, bxyz, st); break;          \
     }                                                                                           \
+  }                                                                                             \
+  int64_t monitored_grid_##P(int64_t nslot, int variant) {                                     \
+    if (P == 0) return nslot / 128;                                                             \
+    switch (variant) {                                                                          \
+      case 1: return nslot / 128;                                                               \
+      case 2: return nslot / 256;                                                               \
+      case 3: return nslot / 512;                                                               \
+      default: return nslot / HLBG_SC_THREADS;                                                  \
+    }                                                                                           \
+  }                                                                                             \
+  void launch_mon_reduce_##P(const double* part, int64_t nparts, double* part2, int64_t n2,      \
+                             int32_t* mon_state, double* result, const SteadyArgs& sa,          \
+                             int steady, cudaStream_t st) {                                      \
+    const int64_t per = (nparts + n2 - 1) / n2;                                                 \
+    k_mon_stage2<<<(unsigned)n2, 256, 0, st>>>(part, nparts, per, part2, n2);                   \
+    k_mon_final<<<1, 256, 0, st>>>(part2, n2, mon_state, result, sa, steady);                   \
   }                                                                                             \
   void launch_iolet_links_##P(const StepArgs& a, const int32_t* rec, const int32_t* rec_slot,    \
                               int64_t n, const int32_t* bxyz, cudaStream_t st) {                \
@@ -789,11 +935,6 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     const int64_t nparts = (ma.nslot + 255) / 256;                                              \
     k_monitor<P><<<(unsigned)nparts, 256, 0, st>>>(ma);                                         \
     k_monitor_final<<<1, 256, 0, st>>>(ma, nparts);                                             \
-  }                                                                                             \
-  void launch_steady_check_##P(const MonitorArgs& ma, const SteadyArgs& sa, cudaStream_t st) {  \
-    const int64_t nparts = (ma.nslot + 255) / 256;                                              \
-    k_monitor<P><<<(unsigned)nparts, 256, 0, st>>>(ma);                                         \
-    k_steady_final<<<1, 256, 0, st>>>(ma, nparts, sa);                                          \
   }                                                                                             \
   void launch_average_##P(const AverageArgs& aa, cudaStream_t st) {                             \
     unsigned g = (unsigned)((aa.nslot + 255) / 256);                                            \

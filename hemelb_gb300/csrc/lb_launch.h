@@ -71,8 +71,8 @@ struct MonitorArgs {
 };
 
 // Steady-state detection after every step (StabilityTester with its convergence
-// check, Code/lb/StabilityTester.h:91-183): the final reduction of the monitor
-// partials counts checks and records the first check whose max |u_new - u_old|
+// check, Code/lb/StabilityTester.h:91-183): the last stage of the fused monitor's
+// reduction counts checks and records the first check whose max |u_new - u_old|
 // is within the threshold (tol * U_ref), and the first unstable one.
 struct SteadyArgs {
   const double* threshold;  // tol * U_ref
@@ -102,7 +102,10 @@ struct AverageArgs {
   void launch_scatter_##P(const GatherArgs& ga, cudaStream_t st);                    \
   void launch_macro_##P(const GatherArgs& ga, cudaStream_t st);                      \
   void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st);          \
-  void launch_steady_check_##P(const MonitorArgs& ma, const SteadyArgs& sa, cudaStream_t st); \
+  int64_t monitored_grid_##P(int64_t nslot, int variant);                                   \
+  void launch_mon_reduce_##P(const double* part, int64_t nparts, double* part2, int64_t n2,    \
+                             int32_t* mon_state, double* result, const SteadyArgs& sa,        \
+                             int steady, cudaStream_t st);                                     \
   void launch_average_##P(const AverageArgs& aa, cudaStream_t st);
 
 HLBG_DECLARE(0)

@@ -315,6 +315,15 @@ class LBM:
             check(rc, self._ctx)
         return a.value, b.value, d.value, rc
 
+    def StepMonitored(self, n: int = 1) -> capi.Stats:
+        """n steps with the fused StabilityTester; the stats of the step before the last
+        (time_step -1 when there is none yet)."""
+        st = capi.Stats()
+        rc = self._lib.hlbg_step_monitored(self._ctx, n, C.byref(st))
+        if rc not in (capi.HLBG_OK, capi.HLBG_ERR_UNSTABLE):
+            check(rc, self._ctx)
+        return st
+
     def AverageTimeLevels(self):
         """Current distributions <- mean of the two time levels (right after a step)."""
         check(self._lib.hlbg_average_time_levels(self._ctx), self._ctx)

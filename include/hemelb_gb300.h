@@ -232,6 +232,16 @@ int hlbg_step_graph(hlbg_ctx *ctx, int32_t nsteps);
 int hlbg_run_to_steady(hlbg_ctx *ctx, double tol, double u_ref, int64_t max_steps,
                        int32_t check_batch, int64_t *steps_to_steady, int64_t *steps_run,
                        double *final_rel_du);
+/* nsteps time steps with the StabilityTester fused into the update (each site's
+ * velocity is recorded as it collides; the change against the previous record,
+ * f > 0 and the mass are reduced on the device).  The check of step k is made while
+ * step k + 1 collides, so the stats returned are those of the step before the last
+ * one (time_step = that step + 1, SimulationState's count when the reference makes
+ * the check), or time_step = -1 when there is none yet: the first step after the
+ * distributions were set or changed outside a monitored step only records.
+ * Replaces hlbg_step + hlbg_reduce per step without re-reading both arrays
+ * (Code/lb/StabilityTester.h:91-183). */
+int hlbg_step_monitored(hlbg_ctx *ctx, int32_t nsteps, hlbg_stats *out);
 /* Replace the current distributions by the mean of the two time levels (valid
  * right after a step, when both arrays hold consecutive states).  No reference
  * counterpart: applied once after the first step of a start from a prescribed

@@ -3,6 +3,7 @@ after every step) and the time-level average, against the oracle in FP64."""
 import numpy as np
 import pytest
 
+from hemelb_gb300 import capi
 from hemelb_gb300.surrogate import Sample
 from oracle.oracle import OracleLBM
 
@@ -29,7 +30,8 @@ def test_run_to_steady_matches_oracle(i):
     s.SetInitialConditions()
     tol = 1e-4
     steps, run, du, rc = s.RunToSteady(tol, ur, 100000, 7)
-    assert rc == 0 and steps <= run < steps + 7
+    # the check of step k is made while step k + 1 collides
+    assert rc == 0 and steps < run <= steps + 7
     o = OracleLBM(g.view, case.params, case.inlets, case.outlets)
     o.set_equilibrium()
     n = 0
@@ -40,9 +42,10 @@ def test_run_to_steady_matches_oracle(i):
             break
         assert n < 100000
     assert n == steps
-    o.step(run - n, 4)
+    o.step(run - 1 - n, 4)
+    assert abs(du - _max_rel_du(o, ur)) <= 1e-12 * du  # the last check: step run - 1
+    o.step(1, 4)
     assert np.array_equal(s.GetFOld(), o.fold())
-    assert abs(du - _max_rel_du(o, ur)) <= 1e-12 * du
     s.close()
 
 
@@ -51,7 +54,6 @@ def test_run_to_steady_reports_timeout():
     s = case.solver()
     s.SetInitialConditions()
     steps, run, du, rc = s.RunToSteady(1e-12, ur, 30, 8)
-    from hemelb_gb300 import capi
     assert rc == capi.HLBG_ERR_TIMEOUT and steps == -1 and run == 30 and du > 0
     s.close()
 
@@ -71,3 +73,34 @@ def test_average_time_levels_matches_oracle():
     o.step(3)
     assert np.array_equal(s.GetFOld(), o.fold())
     s.close()
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32DEV])
+def test_fused_monitor_matches_separate_reduction(prec):
+    """hlbg_step_monitored's stats of step k against hlbg_step + hlbg_reduce after
+    step k on a second context (the same StabilityTester quantities)."""
+    g, case, ur = _small_case(0)
+    a = case.solver(prec)
+    b = case.solver(prec)
+    a.SetInitialConditions()
+    b.SetInitialConditions()
+    assert a.StepMonitored(1).time_step == -1  # the first step only records
+    for k in range(1, 40):
+        sa = a.StepMonitored(1)  # stats of step k
+        b.DoTimeStep(1)
+        sb = b.reduce()  # stats after step k
+        assert sa.time_step == sb.time_step == k + 1
+        if prec == capi.FP64:
+            assert sa.max_du == sb.max_du and sa.min_f == sb.min_f
+            assert abs(sa.mass - sb.mass) <= 1e-12 * sb.mass
+        else:
+            assert abs(sa.max_du - sb.max_du) <= 1e-5 * sb.max_du + 1e-12
+            assert abs(sa.min_f - sb.min_f) <= 1e-6 and abs(sa.mass - sb.mass) <= 1e-9 * sb.mass
+        assert sa.unstable_sites == sb.unstable_sites == 0
+    # the states themselves are the same
+    assert np.array_equal(a.GetFOld(), b.GetFOld())
+    # stepping outside a monitored step invalidates the record
+    a.DoTimeStep(1)
+    assert a.StepMonitored(1).time_step == -1
+    a.close()
+    b.close()
