@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--roots", type=int, default=5)
     ap.add_argument("--box", type=int, default=1280)
     ap.add_argument("--depth", type=int, default=7)
+    ap.add_argument("--root-radius", type=float, default=60.0)
     ap.add_argument("--precision", default="fp32dev", choices=["fp64", "fp32dev", "fp16"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-sites", type=int, default=2_000_000,
@@ -95,9 +96,9 @@ def make_case(args):
     prec = {"fp64": capi.FP64, "fp32dev": capi.FP32DEV, "fp16": capi.FP16}[args.precision]
     if args.workload == "tree":
         c = cases.tree(seed=7, box_sites=args.box, n_roots=args.roots, depth=args.depth,
-                       root_radius=60.0, precision=prec)
-        cfg = {"workload": "random vascular forest, %d trees of depth %d in a %d^3 box of 8^3 blocks"
-               % (args.roots, args.depth, args.box),
+                       root_radius=args.root_radius, precision=prec)
+        cfg = {"workload": "random vascular forest, %d trees of depth %d (root radius %g) in a %d^3 box "
+               "of 8^3 blocks" % (args.roots, args.depth, args.root_radius, args.box),
                "lattice": "D3Q19", "kernel": "TRT (Lambda=3/16)", "wall": "SimpleBounceBack",
                "iolets": "Nash pressure, inlet 1.001 / outlets 1.0", "storage": args.precision,
                "seed": 7}
