@@ -599,6 +599,40 @@ def accuracy_study(net: UNet, samples, box: int, check_every: int = 50, log=None
     return out, summ
 
 
+def bench_kernels(reps: int = 10, batch: int = 4):
+    """CUDA-event time of the convolution kernels at the U-Net's layer shapes on a
+    batch of 96^3 boxes (inputs far larger than L2): TFLOP/s of forward, input
+    gradient and weight gradient, 2 * 27 * C_in * C_out FLOP per voxel each."""
+    shapes = [(96, N_IN, 16), (96, 16, 16), (48, 16, 48), (48, 48, 48), (24, 48, 96), (24, 96, 96),
+              (12, 96, 192), (12, 192, 192), (24, 288, 96), (48, 144, 48), (96, 64, 16)]
+    out = []
+    for dim, cin, cout in shapes:
+        x = torch.randn((batch, dim, dim, dim, cin), device="cuda").to(torch.bfloat16)
+        w = (torch.randn((27, cout, cin), device="cuda") * 0.05).to(torch.bfloat16)
+        b = torch.zeros(cout, device="cuda")
+        y = torch.empty((batch, dim, dim, dim, cout), dtype=torch.bfloat16, device="cuda")
+        dx = torch.empty_like(x)
+        wt = torch.empty((27, cin, cout), dtype=torch.bfloat16, device="cuda")
+        dw = torch.zeros((27, cout, cin), device="cuda")
+        flop = 2.0 * 27 * cin * cout * batch * dim ** 3
+        rec = {"voxels": batch * dim ** 3, "c_in": cin, "c_out": cout}
+        for name, fn in (("forward", lambda: nn.conv3d(x, w, b, y, None, 27, True)),
+                         ("input_grad", lambda: nn.conv3d_data_grad(y, w, dx, None, wt)),
+                         ("weight_grad", lambda: nn.conv3d_weight_grad(x, y, dw))):
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            rec[name] = {"ms": ms, "tflops": flop / ms / 1e9}
+        out.append(rec)
+    return out
+
+
 def main(argv=None):
     """Generate, train, evaluate: the warm-start report as one JSON document."""
     import argparse
@@ -614,8 +648,14 @@ def main(argv=None):
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--out", default="")
     ap.add_argument("--save-weights", default="")
+    ap.add_argument("--bench-kernels", action="store_true",
+                    help="only time the convolution kernels at the network's layer shapes")
     a = ap.parse_args(argv)
     log = lambda m: print(m, flush=True)
+    if a.bench_kernels:
+        res = bench_kernels()
+        log(json.dumps(res, indent=1))
+        return res
     train_s = [Sample.draw(i, box=a.box) for i in range(a.train)]
     test_s = [Sample.draw(1_000_000 + i, box=a.box) for i in range(a.test)]
     t0 = time.perf_counter()
