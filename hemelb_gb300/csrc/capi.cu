@@ -553,7 +553,7 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   parallel_for(nb, [&](int64_t b) {
     int nf = 0;
     for (int w = 0; w < 8; ++w) nf += __builtin_popcountll(mask[b * 8 + w]);
-    packed[b] = nf < 512;
+    packed[b] = HLBG_PACK && nf < 512;
     int j = 0;
     for (int want = 1; want >= 0; --want)  // fluid sites first, then solid ones
       for (int l = 0; l < 512; ++l) {

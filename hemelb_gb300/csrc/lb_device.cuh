@@ -82,6 +82,10 @@ struct IoletDev {
 
 // Flag of a block_nbr entry whose block has its fluid sites packed (slot != site).
 constexpr int32_t kPackedBit = 1 << 30;
+// HLBG_PACK=0 builds the layout and kernels without packing (every slot == site).
+#ifndef HLBG_PACK
+#define HLBG_PACK 1
+#endif
 
 struct StepArgs {
   const void* f_old;

@@ -80,18 +80,42 @@ struct GlobalBase {
 
 // Slot of local site tl in the block of table entry e (e >= 0).
 __device__ __forceinline__ int64_t target_slot(const StepArgs& a, int32_t e, int tl) {
+#if HLBG_PACK
   const int64_t nb = e & ~kPackedBit;
   const int ts = (e & kPackedBit) ? (int)__ldg(a.site2slot + (nb << 9) + tl) : tl;
   return (nb << 9) + ts;
+#else
+  return ((int64_t)e << 9) + tl;
+#endif
 }
 // Element offset of direction D of local site tl in the block of entry e (e >= 0).
 __device__ __forceinline__ int64_t target_off(const StepArgs& a, int32_t e, int D, int tl) {
-  const int64_t ts = target_slot(a, e, tl);
-  return fidx(ts, D);
+#if HLBG_PACK
+  const int32_t nb = e & ~kPackedBit;
+  const int ts = (e & kPackedBit) ? (int)__ldg(a.site2slot + ((int64_t)nb << 9) + tl) : tl;
+  return (int64_t)nb * (Q * kSites) + (D * kSites + ts);
+#else
+  return (int64_t)e * (Q * kSites) + (D * kSites + tl);
+#endif
 }
 // Local site index of slot s (its block's packed flag in `packed`).
 __device__ __forceinline__ int site_of_slot(const StepArgs& a, int64_t s, bool packed) {
+#if HLBG_PACK
   return packed ? (int)__ldg(a.slot2site + s) : (int)(s & (kSites - 1));
+#else
+  return (int)(s & (kSites - 1));
+#endif
+}
+
+// HLBG_PUSH_FENCE=1: keep each push's lookup and store together (no hoisting of
+// the next direction's loads above this store).
+#ifndef HLBG_PUSH_FENCE
+#define HLBG_PUSH_FENCE 0
+#endif
+__device__ __forceinline__ void push_fence() {
+#if HLBG_PUSH_FENCE
+  asm volatile("" ::: "memory");
+#endif
 }
 
 // Per-link dispatch of a site next to a wall or an iolet, unrolled over the 19
@@ -181,6 +205,7 @@ struct PushBulk {
     const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
     const int32_t e = base(k);  // every lane shuffles
     if (store) Store<P>::store(fn, target_off(a, e, D, tl), fpost[D], a);
+    push_fence();
     PushBulk<P, D + 1>::run(fn, a, base, x, y, z, store, fpost);
   }
 };
@@ -236,6 +261,7 @@ struct PushMixed {
       }
     }
     if (st) Store<P>::store(fn, off, v, a);
+    push_fence();
     PushMixed<P, D + 1>::run(fn, a, base, x, y, z, j, own, active, row_fluid, links, r, type, ioid,
                              fpost, m0, mx, my, mz, b, block_xyz);
   }
