@@ -102,6 +102,7 @@ SIGNATURES = {
     "hlbg_run_to_steady": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_int32,
                                      C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "hlbg_average_time_levels": (C.c_int, [C.c_void_p]),
+    "hlbg_set_launch_variant": (C.c_int, [C.c_void_p, C.c_int32]),
     "hlbg_step_monitored": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Stats)]),
     "hlbg_set_block_tau": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_stream_and_collide_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),

@@ -100,6 +100,9 @@ struct hlbg_ctx {
   int32_t* d_block_nbr = nullptr;
   int32_t* d_block_xyz = nullptr;
   uint32_t* d_site_code = nullptr;
+  int32_t* d_warp_block = nullptr;  // fluid-list launch (StepArgs::warp_block)
+  uint16_t* d_lane_slot = nullptr;
+  int64_t n_warps = 0;
   uint16_t* d_slot2site = nullptr;  // packed blocks: local site of each slot
   uint16_t* d_site2slot = nullptr;  // packed blocks: slot of each local site
   std::vector<uint16_t> h_slot2site;
@@ -210,6 +213,9 @@ void fill_args(hlbg_ctx* ctx, StepArgs& a) {
   a.block_nbr = ctx->d_block_nbr;
   a.slot2site = ctx->d_slot2site;
   a.site2slot = ctx->d_site2slot;
+  a.warp_block = ctx->d_warp_block;
+  a.lane_slot = ctx->d_lane_slot;
+  a.n_warps = ctx->n_warps;
   a.site_code = ctx->d_site_code;
   a.block_bulk = ctx->d_block_bulk;
   a.b_wall = ctx->d_b_wall;
@@ -577,6 +583,37 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   ctx->h_slot2site = slot2site;
   // device copies
   int rc;
+  {
+    // Fluid list: per block, its fluid slots in warps of 32 (the last padded with
+    // idle lanes), then its solid slots that share an 8-slot sector with a fluid
+    // slot, in zero-fill warps.
+    std::vector<int32_t> wb;
+    std::vector<uint16_t> ls;
+    std::vector<uint16_t> tmp;
+    auto flush = [&](int64_t b, bool zero) {
+      for (size_t k = 0; k < tmp.size(); k += 32) {
+        wb.push_back(zero ? (int32_t)((uint32_t)b | 0x80000000u) : (int32_t)b);
+        for (size_t t = k; t < k + 32; ++t) ls.push_back(t < tmp.size() ? tmp[t] : (uint16_t)0xffff);
+      }
+      tmp.clear();
+    };
+    for (int64_t b = 0; b < nb; ++b) {
+      for (int j = 0; j < 512; ++j)
+        if (code[b * 512 + j]) tmp.push_back((uint16_t)j);
+      flush(b, false);
+      for (int sec = 0; sec < 64; ++sec) {
+        bool any = false;
+        for (int t = 0; t < 8; ++t) any |= code[b * 512 + sec * 8 + t] != 0;
+        if (!any) continue;
+        for (int t = 0; t < 8; ++t)
+          if (!code[b * 512 + sec * 8 + t]) tmp.push_back((uint16_t)(sec * 8 + t));
+      }
+      flush(b, true);
+    }
+    ctx->n_warps = (int64_t)wb.size();
+    if ((rc = upload(ctx, &ctx->d_warp_block, wb))) return rc;
+    if ((rc = upload(ctx, &ctx->d_lane_slot, ls))) return rc;
+  }
   if ((rc = upload(ctx, &ctx->d_block_nbr, bnbr))) return rc;
   if ((rc = upload(ctx, &ctx->d_slot2site, slot2site))) return rc;
   if ((rc = upload(ctx, &ctx->d_site2slot, site2slot))) return rc;
@@ -640,9 +677,9 @@ int mon_invalidate(hlbg_ctx* ctx) {
 
 int64_t monitored_grid(const hlbg_ctx* ctx) {
   switch (ctx->prec) {
-    case 0: return monitored_grid_0(ctx->nslot, ctx->sc_variant);
-    case 1: return monitored_grid_1(ctx->nslot, ctx->sc_variant);
-    default: return monitored_grid_2(ctx->nslot, ctx->sc_variant);
+    case 0: return monitored_grid_0(ctx->nslot, ctx->sc_variant, ctx->n_warps);
+    case 1: return monitored_grid_1(ctx->nslot, ctx->sc_variant, ctx->n_warps);
+    default: return monitored_grid_2(ctx->nslot, ctx->sc_variant, ctx->n_warps);
   }
 }
 
@@ -770,7 +807,8 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_io_tab,    ctx->d_stage,     ctx->d_stage_rho, ctx->d_stage_u,
                   ctx->d_list,      ctx->d_part,      ctx->d_part_bad,  ctx->d_steady,
                   ctx->d_steady_n,  ctx->d_slot2site, ctx->d_site2slot, ctx->d_mon_u,
-                  ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result};
+                  ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result,
+                  ctx->d_warp_block, ctx->d_lane_slot};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
@@ -1169,7 +1207,9 @@ int hlbg_autotune(hlbg_ctx* ctx, int32_t steps_per_trial, int32_t* chosen, float
   if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
   int best = ctx->sc_variant;
   float best_t = 1e30f;
-  for (int v = 0; v < (ctx->prec == 0 ? 1 : kSCVariants); ++v) {
+  static const int kFp64Variants[2] = {0, 5};
+  for (int k = 0; k < (ctx->prec == 0 ? 2 : kSCVariants); ++k) {
+    const int v = ctx->prec == 0 ? kFp64Variants[k] : k;
     ctx->sc_variant = v;
     int rc = hlbg_step(ctx, 1, nullptr);
     if (rc) return rc;
@@ -1185,6 +1225,14 @@ int hlbg_autotune(hlbg_ctx* ctx, int32_t steps_per_trial, int32_t* chosen, float
   ctx->graphs.clear();
   if (chosen) *chosen = best;
   if (best_ms) *best_ms = best_t / steps_per_trial;
+  return HLBG_OK;
+}
+
+int hlbg_set_launch_variant(hlbg_ctx* ctx, int32_t variant) {
+  if (!ctx || variant < 0 || variant >= kSCVariants) return HLBG_ERR_INVAL;
+  ctx->sc_variant = variant;
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);  // captured launches changed
+  ctx->graphs.clear();
   return HLBG_OK;
 }
 

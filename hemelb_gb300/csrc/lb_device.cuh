@@ -103,6 +103,12 @@ struct StepArgs {
   double* mon_part;
   int64_t mon_nparts;
   const int32_t* mon_state;
+  // Fluid-list launch: warp w works on block warp_block[w] & 0x7fffffff, lane k on
+  // its slot lane_slot[32 w + k] (0xffff: idle); a negative warp_block marks a warp
+  // that only writes zeros into the solid slots sharing a 32-byte sector with fluid.
+  const int32_t* warp_block;
+  const uint16_t* lane_slot;
+  int64_t n_warps;
   const uint32_t* site_code;
   const uint8_t* block_bulk;  // 1: all 512 slots are bulk sites
   const uint32_t* b_wall;

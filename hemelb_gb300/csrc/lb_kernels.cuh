@@ -451,6 +451,88 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
   }
 }
 
+// One warp of the fluid list: 32 fluid sites of one block (or the zero-fill of its
+// solid slots that share sectors with fluid), so no lane is spent on a solid slot.
+template <int P, bool MON>
+__device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w,
+                                                    const int32_t* __restrict__ block_xyz, MonAcc& acc,
+                                                    bool check) {
+  using St = Store<P>;
+  using S = typename St::S;
+  using T = typename Calc<P>::T;
+  if (w >= a.n_warps) return;  // whole warp
+  const int lane = threadIdx.x & 31;
+  const int32_t e = __ldg(a.warp_block + w);
+  const int64_t b = e & 0x7fffffff;
+  const unsigned js = __ldg(a.lane_slot + w * 32 + lane);
+  const bool on = js != 0xffffu;
+  const int j = on ? (int)js : 0;
+  const int64_t s = b * kSites + j;
+  S* fn = static_cast<S*>(a.f_new);
+  if (e < 0) {  // zero-fill warp: complete the sectors its slots share with fluid
+    if (on) {
+#pragma unroll
+      for (int d = 0; d < Q; ++d) St::store(fn, fidx(s, d), (T)0, a);
+    }
+    return;
+  }
+  const int32_t* tab = a.block_nbr + b * 27;
+  const int32_t tabreg = lane < 27 ? __ldg(tab + lane) : 0;
+  const uint32_t code = on ? (a.block_bulk[b] ? 1u : a.site_code[s]) : 0u;
+  const bool packed = (__shfl_sync(0xffffffffu, tabreg, 13) & kPackedBit) != 0;
+  const int l = on ? site_of_slot(a, s, packed) : 0;
+  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + j;
+  T f[Q], fpost[Q];
+  if (code != 0) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
+  } else {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = (T)(P == 0 ? weight_d(i) : 0.0);
+  }
+  T m0, mx, my, mz;
+  collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
+  if constexpr (MON) {
+    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check);
+  }
+  const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
+  const bool bnd = code >= 2;
+  if (__ballot_sync(0xffffffffu, bnd) == 0) {
+    PushBulk<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, code == 1, fpost);
+  } else {
+    const int64_t r = bnd ? (int64_t)code - 2 : 0;
+    const uint64_t links = bnd ? a.b_links[r] : 0ull;
+    const int type = bnd ? (int)a.b_type[r] : 0;
+    const int ioid = bnd ? a.b_ioid[r] : 0;
+    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, j, b * (Q * kSites), code != 0, false, links,
+                         r, type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
+  }
+}
+
+template <int P, int THREADS, int MINB, bool MON>
+__global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArgs a, const int32_t* block_xyz) {
+  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  bool check = false;
+  if constexpr (MON) check = *a.mon_state != 0;
+  collide_listed_warp<P, MON>(a, ((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5, block_xyz, acc, check);
+  if constexpr (MON) {
+    acc = mon_block(acc);
+    if (threadIdx.x == 0) {
+      const int64_t n = a.mon_nparts;
+      a.mon_part[blockIdx.x] = acc.mass;
+      a.mon_part[n + blockIdx.x] = acc.maxdu;
+      a.mon_part[2 * n + blockIdx.x] = acc.minf;
+      a.mon_part[3 * n + blockIdx.x] = (double)acc.bad;
+    }
+  }
+}
+
+template <int P, int THREADS, int MINB, bool MON>
+void launch_listed(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
+  const int64_t g = (a.n_warps * 32 + THREADS - 1) / THREADS;
+  if (g) k_stream_collide_listed<P, THREADS, MINB, MON><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
+}
+
 // All slots.  THREADS threads per CTA with at least MINB CTAs resident per SM;
 // PERSIST: a grid of resident CTAs striding over 128-slot chunks in order, else
 // one thread per slot.  The variants are the autotuner's candidates.
@@ -891,6 +973,16 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       if (g) k_stream_collide_list<P><<<g, 256, 0, st>>>(a, bxyz);                              \
       return;                                                                                   \
     }                                                                                           \
+    if (variant == 5) {                                                                         \
+      if (a.mon_u) launch_listed<P, 128, (P == 0 ? 2 : 10), true>(a, bxyz, st);                 \
+      else launch_listed<P, 128, (P == 0 ? 2 : 10), false>(a, bxyz, st);                        \
+      return;                                                                                   \
+    }                                                                                           \
+    if (variant == 6) {                                                                         \
+      if (a.mon_u) launch_listed<P, 128, (P == 0 ? 2 : 8), true>(a, bxyz, st);                  \
+      else launch_listed<P, 128, (P == 0 ? 2 : 8), false>(a, bxyz, st);                         \
+      return;                                                                                   \
+    }                                                                                           \
     if (P == 0) variant = -1;                                                                   \
     if (a.mon_u) { /* one partial per CTA: the persistent shape is not used */                  \
       switch (variant) {                                                                        \
@@ -911,7 +1003,8 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       default: launch_sc<P, HLBG_SC_THREADS, HLBG_SC_MINB, false>(a, bxyz, st); break;          \
     }                                                                                           \
   }                                                                                             \
-  int64_t monitored_grid_##P(int64_t nslot, int variant) {                                     \
+  int64_t monitored_grid_##P(int64_t nslot, int variant, int64_t n_warps) {                    \
+    if (variant == 5 || variant == 6) return (n_warps * 32 + 127) / 128;                        \
     if (P == 0) return nslot / 128;                                                             \
     switch (variant) {                                                                          \
       case 1: return nslot / 128;                                                               \

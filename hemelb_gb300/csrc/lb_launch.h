@@ -12,7 +12,7 @@ struct StepArgs;
 // Launch variants of the stream-and-collide kernel (FP32 / FP16 forms; FP64 has one):
 // 0 default shape, 1: 128x8, 2: 256x4, 3: 512x2 threads x resident CTAs per SM,
 // 4: persistent 128-thread CTAs striding over the slots.
-constexpr int kSCVariants = 5;
+constexpr int kSCVariants = 7;  // 5, 6: the fluid-list launch
 
 struct PostArgs {
   void* f_new;
@@ -102,7 +102,7 @@ struct AverageArgs {
   void launch_scatter_##P(const GatherArgs& ga, cudaStream_t st);                    \
   void launch_macro_##P(const GatherArgs& ga, cudaStream_t st);                      \
   void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st);          \
-  int64_t monitored_grid_##P(int64_t nslot, int variant);                                   \
+  int64_t monitored_grid_##P(int64_t nslot, int variant, int64_t n_warps);                                   \
   void launch_mon_reduce_##P(const double* part, int64_t nparts, double* part2, int64_t n2,    \
                              int32_t* mon_state, double* result, const SteadyArgs& sa,        \
                              int steady, cudaStream_t st);                                     \

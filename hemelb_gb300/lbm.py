@@ -328,6 +328,9 @@ class LBM:
         """Current distributions <- mean of the two time levels (right after a step)."""
         check(self._lib.hlbg_average_time_levels(self._ctx), self._ctx)
 
+    def SetLaunchVariant(self, variant: int):
+        check(self._lib.hlbg_set_launch_variant(self._ctx, variant), self._ctx)
+
     def autotune(self, steps_per_trial: int = 5):
         v = C.c_int32()
         ms = C.c_float()
