@@ -560,6 +560,13 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     int nf = 0;
     for (int w = 0; w < 8; ++w) nf += __builtin_popcountll(mask[b * 8 + w]);
     packed[b] = HLBG_PACK && nf < 512;
+    if (!packed[b]) {  // slot == site
+      for (int l = 0; l < 512; ++l) {
+        site2slot[b * 512 + l] = (uint16_t)l;
+        slot2site[b * 512 + l] = (uint16_t)l;
+      }
+      return;
+    }
     int j = 0;
     for (int want = 1; want >= 0; --want)  // fluid sites first, then solid ones
       for (int l = 0; l < 512; ++l) {
@@ -655,7 +662,10 @@ int mon_prepare(hlbg_ctx* ctx) {
   int rc = dev_alloc(ctx, &u, 3 * (size_t)ctx->nslot * es);
   if (rc) return rc;
   ctx->d_mon_u = u;
-  if ((rc = dev_alloc(ctx, &ctx->d_mon_part, 4 * (size_t)(ctx->nslot / 128)))) return rc;
+  // one partial per CTA of 128 or more threads, for every launch shape: all slots,
+  // or the fluid list (whose padded warps can outnumber a block's 16)
+  const int64_t max_ctas = (std::max(ctx->nslot, ctx->n_warps * 32) + 127) / 128;
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_part, 4 * (size_t)max_ctas))) return rc;
   if ((rc = dev_alloc(ctx, &ctx->d_mon_part2, 4 * (size_t)kMonStage2))) return rc;
   if ((rc = dev_alloc(ctx, &ctx->d_mon_state, 1))) return rc;
   if ((rc = dev_alloc(ctx, &ctx->d_mon_result, 5))) return rc;
