@@ -60,6 +60,13 @@ class Stats(C.Structure):
     ]
 
 
+class Incomp(C.Structure):
+    _fields_ = [
+        ("min_density", C.c_double), ("max_density", C.c_double), ("max_velocity", C.c_double),
+        ("max_relative_density_difference", C.c_double), ("time_step", C.c_int64),
+    ]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "hlbg_synth_pipe": (C.c_int, [C.c_double, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
@@ -104,6 +111,7 @@ SIGNATURES = {
     "hlbg_average_time_levels": (C.c_int, [C.c_void_p]),
     "hlbg_set_launch_variant": (C.c_int, [C.c_void_p, C.c_int32]),
     "hlbg_step_monitored": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Stats)]),
+    "hlbg_incompressibility": (C.c_int, [C.c_void_p, C.POINTER(Incomp)]),
     "hlbg_set_block_tau": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_stream_and_collide_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "hlbg_post_step_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),

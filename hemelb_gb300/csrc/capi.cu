@@ -653,6 +653,8 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
 }
 
 constexpr int64_t kMonStage2 = 1024;
+constexpr int kMonFields = 7;  // partials: mass, max |du|, min f, unstable, min rho, max rho, max |u|
+constexpr int kMonResult = 8;  // the same plus the valid flag
 
 // Buffers of the fused StabilityTester, allocated on first use.
 int mon_prepare(hlbg_ctx* ctx) {
@@ -665,11 +667,11 @@ int mon_prepare(hlbg_ctx* ctx) {
   // one partial per CTA of 128 or more threads, for every launch shape: all slots,
   // or the fluid list (whose padded warps can outnumber a block's 16)
   const int64_t max_ctas = (std::max(ctx->nslot, ctx->n_warps * 32) + 127) / 128;
-  if ((rc = dev_alloc(ctx, &ctx->d_mon_part, 4 * (size_t)max_ctas))) return rc;
-  if ((rc = dev_alloc(ctx, &ctx->d_mon_part2, 4 * (size_t)kMonStage2))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_part, kMonFields * (size_t)max_ctas))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_part2, kMonFields * (size_t)kMonStage2))) return rc;
   if ((rc = dev_alloc(ctx, &ctx->d_mon_state, 1))) return rc;
-  if ((rc = dev_alloc(ctx, &ctx->d_mon_result, 5))) return rc;
-  CK(cudaMallocHost((void**)&ctx->h_mon_result, 5 * sizeof(double)));
+  if ((rc = dev_alloc(ctx, &ctx->d_mon_result, kMonResult))) return rc;
+  CK(cudaMallocHost((void**)&ctx->h_mon_result, kMonResult * sizeof(double)));
   CK(cudaMemsetAsync(ctx->d_mon_state, 0, sizeof(int32_t), ctx->stream));
   ctx->mon_recorded = false;
   return HLBG_OK;
@@ -1173,7 +1175,7 @@ int hlbg_step_monitored(hlbg_ctx* ctx, int32_t nsteps, hlbg_stats* out) {
     }
     done += n;
   }
-  CK(cudaMemcpyAsync(ctx->h_mon_result, ctx->d_mon_result, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->h_mon_result, ctx->d_mon_result, kMonResult * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const double* r = ctx->h_mon_result;
   const bool valid = r[4] != 0.0;
@@ -1183,6 +1185,23 @@ int hlbg_step_monitored(hlbg_ctx* ctx, int32_t nsteps, hlbg_stats* out) {
   out->unstable_sites = valid ? (int64_t)r[3] : 0;
   out->time_step = valid ? (int64_t)ctx->t1 - 1 : -1;
   return valid && r[3] > 0.0 ? HLBG_ERR_UNSTABLE : HLBG_OK;
+}
+
+int hlbg_incompressibility(hlbg_ctx* ctx, hlbg_incomp* out) {
+  if (!ctx || !out) return HLBG_ERR_INVAL;
+  if (!ctx->d_mon_result) return fail(ctx, HLBG_ERR_STATE, "no monitored step yet");
+  CK(cudaMemcpyAsync(ctx->h_mon_result, ctx->d_mon_result, kMonResult * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const double* r = ctx->h_mon_result;
+  const bool valid = r[4] != 0.0;
+  out->min_density = valid ? r[5] : 0.0;
+  out->max_density = valid ? r[6] : 0.0;
+  out->max_velocity = valid ? r[7] : 0.0;
+  // IncompressibilityChecker::GetMaxRelativeDensityDifference, REFERENCE_DENSITY = 1
+  out->max_relative_density_difference = valid ? r[6] - r[5] : 0.0;
+  out->time_step = valid ? (int64_t)ctx->t1 - 1 : -1;
+  return HLBG_OK;
 }
 
 int hlbg_average_time_levels(hlbg_ctx* ctx) {

@@ -277,16 +277,27 @@ struct PushMixed<P, Q> {
 // StabilityTester::PostSendToParent (Code/lb/StabilityTester.h:91-149) and
 // ComputeRelativeDifference (:160-183) plus total mass: one slot per thread, one
 // partial per CTA, reduced by k_monitor_final in a fixed order (deterministic).
+// The fused monitor also tracks IncompressibilityChecker's quantities
+// (Code/lb/IncompressibilityChecker.hpp:157-199): smallest and largest density and
+// largest velocity magnitude over the sites.
 struct MonAcc {
   double mass, maxdu, minf;
   unsigned long long bad;
+  double rmin, rmax, umax;
 };
+
+__device__ __forceinline__ MonAcc mon_neutral() {
+  return MonAcc{0.0, 0.0, 1.0e300, 0ull, 1.0e300, -1.0e300, 0.0};
+}
 
 __device__ __forceinline__ void mon_combine(MonAcc& a, const MonAcc& b) {
   a.mass += b.mass;
   if (!(b.maxdu <= a.maxdu)) a.maxdu = b.maxdu;  // NaN-propagating max
   a.minf = fmin(a.minf, b.minf);
   a.bad += b.bad;
+  a.rmin = fmin(a.rmin, b.rmin);
+  a.rmax = fmax(a.rmax, b.rmax);
+  if (!(b.umax <= a.umax)) a.umax = b.umax;
 }
 
 __device__ __forceinline__ MonAcc mon_shfl(const MonAcc& v, int off) {
@@ -295,6 +306,9 @@ __device__ __forceinline__ MonAcc mon_shfl(const MonAcc& v, int off) {
   o.maxdu = __shfl_down_sync(0xffffffffu, v.maxdu, off);
   o.minf = __shfl_down_sync(0xffffffffu, v.minf, off);
   o.bad = __shfl_down_sync(0xffffffffu, v.bad, off);
+  o.rmin = __shfl_down_sync(0xffffffffu, v.rmin, off);
+  o.rmax = __shfl_down_sync(0xffffffffu, v.rmax, off);
+  o.umax = __shfl_down_sync(0xffffffffu, v.umax, off);
   return o;
 }
 
@@ -306,7 +320,7 @@ __device__ __forceinline__ MonAcc mon_block(MonAcc v) {
   if (lane == 0) sh[w] = v;
   __syncthreads();
   if (w == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : MonAcc{0.0, 0.0, 1.0e300, 0ull};
+    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : mon_neutral();
     for (int off = 16; off > 0; off >>= 1) mon_combine(v, mon_shfl(v, off));
   }
   return v;
@@ -332,6 +346,10 @@ __device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const typ
       const double du = sqrt(dot3d(dx, dy, dz, dx, dy, dz));
       if (!(du <= acc.maxdu)) acc.maxdu = du;
       acc.mass += m0;
+      acc.rmin = fmin(acc.rmin, m0);
+      acc.rmax = fmax(acc.rmax, m0);
+      const double um = sqrt(dot3d(ux, uy, uz, ux, uy, uz));
+      if (!(um <= acc.umax)) acc.umax = um;
       bool bad = false;
       double mn = f[0];
 #pragma unroll
@@ -354,6 +372,10 @@ __device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const typ
       const double du = (double)sqrtf(dx * dx + dy * dy + dz * dz);
       if (!(du <= acc.maxdu)) acc.maxdu = du;
       acc.mass += 1.0 + (double)m0;
+      acc.rmin = fmin(acc.rmin, 1.0 + (double)m0);
+      acc.rmax = fmax(acc.rmax, 1.0 + (double)m0);
+      const double um = (double)sqrtf(ux * ux + uy * uy + uz * uz);
+      if (!(um <= acc.umax)) acc.umax = um;
       bool bad = false;
       float mn = 1.0e30f;
 #pragma unroll
@@ -523,6 +545,9 @@ __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArg
       a.mon_part[n + blockIdx.x] = acc.maxdu;
       a.mon_part[2 * n + blockIdx.x] = acc.minf;
       a.mon_part[3 * n + blockIdx.x] = (double)acc.bad;
+      a.mon_part[4 * n + blockIdx.x] = acc.rmin;
+      a.mon_part[5 * n + blockIdx.x] = acc.rmax;
+      a.mon_part[6 * n + blockIdx.x] = acc.umax;
     }
   }
 }
@@ -557,6 +582,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
       a.mon_part[n + blockIdx.x] = acc.maxdu;
       a.mon_part[2 * n + blockIdx.x] = acc.minf;
       a.mon_part[3 * n + blockIdx.x] = (double)acc.bad;
+      a.mon_part[4 * n + blockIdx.x] = acc.rmin;
+      a.mon_part[5 * n + blockIdx.x] = acc.rmax;
+      a.mon_part[6 * n + blockIdx.x] = acc.umax;
     }
   }
 }
@@ -569,7 +597,8 @@ static __global__ void __launch_bounds__(256) k_mon_stage2(const double* __restr
   MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
   const int64_t lo = (int64_t)blockIdx.x * per, hi = lo + per < n_in ? lo + per : n_in;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-    mon_combine(acc, MonAcc{in[i], in[n_in + i], in[2 * n_in + i], (unsigned long long)in[3 * n_in + i]});
+    mon_combine(acc, MonAcc{in[i], in[n_in + i], in[2 * n_in + i], (unsigned long long)in[3 * n_in + i],
+                            in[4 * n_in + i], in[5 * n_in + i], in[6 * n_in + i]});
   __syncthreads();
   acc = mon_block(acc);
   if (threadIdx.x == 0) {
@@ -577,10 +606,14 @@ static __global__ void __launch_bounds__(256) k_mon_stage2(const double* __restr
     out[n_out + blockIdx.x] = acc.maxdu;
     out[2 * n_out + blockIdx.x] = acc.minf;
     out[3 * n_out + blockIdx.x] = (double)acc.bad;
+    out[4 * n_out + blockIdx.x] = acc.rmin;
+    out[5 * n_out + blockIdx.x] = acc.rmax;
+    out[6 * n_out + blockIdx.x] = acc.umax;
   }
 }
 
-// Last stage: result = [mass, max |du|, min f, unstable, valid]; valid is 0 for the
+// Last stage: result = [mass, max |du|, min f, unstable, valid, min rho, max rho,
+// max |u|]; valid is 0 for the
 // first step after the state was set (it only recorded velocities).  With sa, a
 // valid check is also counted for steady-state detection.
 // Every step then marks the recorded velocities as present.
@@ -589,7 +622,8 @@ static __global__ void __launch_bounds__(256) k_mon_final(const double* __restri
                                                           SteadyArgs sa, int steady) {
   MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
-    mon_combine(acc, MonAcc{part[i], part[n + i], part[2 * n + i], (unsigned long long)part[3 * n + i]});
+    mon_combine(acc, MonAcc{part[i], part[n + i], part[2 * n + i], (unsigned long long)part[3 * n + i],
+                            part[4 * n + i], part[5 * n + i], part[6 * n + i]});
   __syncthreads();
   acc = mon_block(acc);
   if (threadIdx.x == 0) {
@@ -599,6 +633,9 @@ static __global__ void __launch_bounds__(256) k_mon_final(const double* __restri
     result[2] = acc.minf;
     result[3] = (double)acc.bad;
     result[4] = valid;
+    result[5] = acc.rmin;
+    result[6] = acc.rmax;
+    result[7] = acc.umax;
     if (steady && valid) {
       const long long k = sa.counters[0] + 1;
       sa.counters[0] = k;
@@ -910,7 +947,8 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
 static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, int64_t nparts) {
   MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
   for (int64_t i = threadIdx.x; i < nparts; i += blockDim.x)
-    mon_combine(acc, MonAcc{ma.part_mass[i], ma.part_max[i], ma.part_min[i], ma.part_bad[i]});
+    mon_combine(acc, MonAcc{ma.part_mass[i], ma.part_max[i], ma.part_min[i], ma.part_bad[i], 1.0e300, -1.0e300,
+                            0.0});
   __syncthreads();
   acc = mon_block(acc);
   if (threadIdx.x == 0) {
@@ -973,9 +1011,11 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       if (g) k_stream_collide_list<P><<<g, 256, 0, st>>>(a, bxyz);                              \
       return;                                                                                   \
     }                                                                                           \
+    /* monitored steps carry more live values: the 10-CTA shapes become 8-CTA ones */            \
+    if (a.mon_u && (variant == 0 || variant == 4)) variant = 1;                                  \
+    if (a.mon_u && variant == 5) variant = 6;                                                   \
     if (variant == 5) {                                                                         \
-      if (a.mon_u) launch_listed<P, 128, (P == 0 ? 2 : 10), true>(a, bxyz, st);                 \
-      else launch_listed<P, 128, (P == 0 ? 2 : 10), false>(a, bxyz, st);                        \
+      launch_listed<P, 128, (P == 0 ? 2 : 10), false>(a, bxyz, st);                             \
       return;                                                                                   \
     }                                                                                           \
     if (variant == 6) {                                                                         \
@@ -986,11 +1026,10 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     if (P == 0) variant = -1;                                                                   \
     if (a.mon_u) { /* one partial per CTA: the persistent shape is not used */                  \
       switch (variant) {                                                                        \
-        case 1: launch_sc<P, 128, (P == 0 ? 2 : 8), false, true>(a, bxyz, st); break;           \
         case 2: launch_sc<P, 256, (P == 0 ? 2 : 4), false, true>(a, bxyz, st); break;           \
         case 3: launch_sc<P, 512, (P == 0 ? 1 : 2), false, true>(a, bxyz, st); break;           \
         case -1: launch_sc<P, 128, 2, false, true>(a, bxyz, st); break;                         \
-        default: launch_sc<P, HLBG_SC_THREADS, HLBG_SC_MINB, false, true>(a, bxyz, st); break;  \
+        default: launch_sc<P, 128, (P == 0 ? 2 : 8), false, true>(a, bxyz, st); break;          \
       }                                                                                         \
       return;                                                                                   \
     }                                                                                           \
@@ -1010,7 +1049,7 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       case 1: return nslot / 128;                                                               \
       case 2: return nslot / 256;                                                               \
       case 3: return nslot / 512;                                                               \
-      default: return nslot / HLBG_SC_THREADS;                                                  \
+      default: return nslot / 128; /* monitored steps: the 128 x 8 shape */                     \
     }                                                                                           \
   }                                                                                             \
   void launch_mon_reduce_##P(const double* part, int64_t nparts, double* part2, int64_t n2,      \

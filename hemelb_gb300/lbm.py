@@ -324,6 +324,12 @@ class LBM:
             check(rc, self._ctx)
         return st
 
+    def Incompressibility(self) -> capi.Incomp:
+        """IncompressibilityChecker's quantities of the last monitored step."""
+        out = capi.Incomp()
+        check(self._lib.hlbg_incompressibility(self._ctx, C.byref(out)), self._ctx)
+        return out
+
     def AverageTimeLevels(self):
         """Current distributions <- mean of the two time levels (right after a step)."""
         check(self._lib.hlbg_average_time_levels(self._ctx), self._ctx)

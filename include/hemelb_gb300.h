@@ -129,6 +129,16 @@ typedef struct hlbg_stats {
   int64_t time_step;       /* 1-indexed SimulationState time step of the next update */
 } hlbg_stats;
 
+/* IncompressibilityChecker's quantities (Code/lb/IncompressibilityChecker.hpp:
+ * 157-199) for the state checked by the last monitored step. */
+typedef struct hlbg_incomp {
+  double min_density;                       /* GetGlobalSmallestDensity */
+  double max_density;                       /* GetGlobalLargestDensity */
+  double max_velocity;                      /* GetGlobalLargestVelocityMagnitude */
+  double max_relative_density_difference;   /* (max - min) / reference density 1 */
+  int64_t time_step;                        /* as hlbg_stats; -1 when none */
+} hlbg_incomp;
+
 typedef struct hlbg_ctx hlbg_ctx;
 
 /* ---- geometry: synthetic generators (seeded, deterministic) ---------------- */
@@ -242,6 +252,12 @@ int hlbg_run_to_steady(hlbg_ctx *ctx, double tol, double u_ref, int64_t max_step
  * Replaces hlbg_step + hlbg_reduce per step without re-reading both arrays
  * (Code/lb/StabilityTester.h:91-183). */
 int hlbg_step_monitored(hlbg_ctx *ctx, int32_t nsteps, hlbg_stats *out);
+/* IncompressibilityChecker for the state checked by the last monitored step
+ * (hlbg_step_monitored or hlbg_run_to_steady): the densities and velocities are
+ * those of the state each site collided, as the reference's property cache holds
+ * them after a step.  IsDensityDiffWithinRange is
+ * max_relative_density_difference < 0.05 with the reference's default. */
+int hlbg_incompressibility(hlbg_ctx *ctx, hlbg_incomp *out);
 /* Replace the current distributions by the mean of the two time levels (valid
  * right after a step, when both arrays hold consecutive states).  No reference
  * counterpart: applied once after the first step of a start from a prescribed

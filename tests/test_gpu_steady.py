@@ -105,3 +105,30 @@ def test_fused_monitor_matches_separate_reduction(prec):
     assert a.StepMonitored(1).time_step == -1
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32DEV])
+def test_incompressibility_checker_of_the_monitored_state(prec):
+    """IncompressibilityChecker's min / max density and max velocity magnitude
+    (Code/lb/IncompressibilityChecker.hpp:157-199) of the state the last monitored
+    step collided, against the macroscopic fields of that state."""
+    g, case, ur = _small_case(1)
+    a = case.solver(prec)
+    b = case.solver(prec)
+    a.SetInitialConditions()
+    b.SetInitialConditions()
+    a.StepMonitored(1)
+    assert a.Incompressibility().time_step == -1
+    for k in range(1, 30):
+        a.StepMonitored(1)  # collides state k
+        b.DoTimeStep(1)     # state k
+        inc = a.Incompressibility()
+        rho, u = b.macro()
+        umag = np.sqrt((u * u).sum(axis=1))
+        tol = 1e-14 if prec == capi.FP64 else 1e-6
+        assert inc.time_step == k + 1
+        assert abs(inc.min_density - rho.min()) <= tol and abs(inc.max_density - rho.max()) <= tol
+        assert abs(inc.max_velocity - umag.max()) <= tol * max(1.0, umag.max()) + (0 if prec == capi.FP64 else 1e-7)
+        assert abs(inc.max_relative_density_difference - (inc.max_density - inc.min_density)) <= 1e-15
+    a.close()
+    b.close()
