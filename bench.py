@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--box", type=int, default=1280)
     ap.add_argument("--depth", type=int, default=7)
     ap.add_argument("--root-radius", type=float, default=60.0)
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="launch shape of the update (hlbg_set_launch_variant); -1: autotune")
     ap.add_argument("--precision", default="fp32dev", choices=["fp64", "fp32dev", "fp16"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-sites", type=int, default=2_000_000,
@@ -291,7 +293,11 @@ def main():
     n = lbm.n_sites
     lbm.SetInitialConditions()
     # launch shape picked by the library's autotuner (its trial steps are warm-up)
-    variant, tuned_ms = lbm.autotune(3)
+    if args.variant < 0:
+        variant, tuned_ms = lbm.autotune(3)
+    else:
+        variant = args.variant
+        lbm.SetLaunchVariant(variant)
     lbm.DoTimeStep(args.warmup)
     # ---- device-resident timed region ---------------------------------------
     sampler = ClockSampler()

@@ -622,8 +622,10 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     if ((rc = upload(ctx, &ctx->d_lane_slot, ls))) return rc;
   }
   if ((rc = upload(ctx, &ctx->d_block_nbr, bnbr))) return rc;
-  if ((rc = upload(ctx, &ctx->d_slot2site, slot2site))) return rc;
-  if ((rc = upload(ctx, &ctx->d_site2slot, site2slot))) return rc;
+  if (HLBG_PACK) {  // the kernels read the tables only in packed builds
+    if ((rc = upload(ctx, &ctx->d_slot2site, slot2site))) return rc;
+    if ((rc = upload(ctx, &ctx->d_site2slot, site2slot))) return rc;
+  }
   if ((rc = upload(ctx, &ctx->d_block_xyz, ctx->h_block_xyz))) return rc;
   if ((rc = upload(ctx, &ctx->d_site_code, code))) return rc;
   if ((rc = upload(ctx, &ctx->d_block_bulk, bulk))) return rc;

@@ -82,9 +82,11 @@ struct IoletDev {
 
 // Flag of a block_nbr entry whose block has its fluid sites packed (slot != site).
 constexpr int32_t kPackedBit = 1 << 30;
-// HLBG_PACK=0 builds the layout and kernels without packing (every slot == site).
+// HLBG_PACK=1 builds the packed layout (fluid sites of partly fluid blocks in the
+// first slots).  It moves 5-12% fewer bytes but the slot lookups of the pushes cost
+// more than that saves (measured on the vascular forest), so the default is off.
 #ifndef HLBG_PACK
-#define HLBG_PACK 1
+#define HLBG_PACK 0
 #endif
 
 struct StepArgs {
