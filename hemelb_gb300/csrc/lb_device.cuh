@@ -156,6 +156,10 @@ struct Store<0> {
 #ifndef HLBG_STREAM_LOADS
 #define HLBG_STREAM_LOADS 0
 #endif
+// HLBG_STREAM_STORES=1: cache-streaming stores (st.global.cs) for the new array.
+#ifndef HLBG_STREAM_STORES
+#define HLBG_STREAM_STORES 0
+#endif
 template <>
 struct Store<1> {
   using S = float;
@@ -167,7 +171,11 @@ struct Store<1> {
 #endif
   }
   static __device__ __forceinline__ void store(S* p, int64_t i, float v, const StepArgs&) {
+#if HLBG_STREAM_STORES
+    __stcs(p + i, v);
+#else
     p[i] = v;
+#endif
   }
 };
 template <>

@@ -130,7 +130,8 @@ struct BoundaryAll {
     constexpr int inv = Lat::inv(D);
     const int64_t own = fidx(s, 0) - (int64_t)(s & (kSites - 1));  // this block's element base
     const int l = (int)(s & (kSites - 1));  // this site's slot in its block
-    if (D > 0 && type >= 2 && ((im >> (D - 1)) & 1u)) {
+    constexpr int db = D > 0 ? D - 1 : 0, ib = inv > 0 ? inv - 1 : 0;  // bit of D, of its inverse
+    if (D > 0 && type >= 2 && ((im >> db) & 1u)) {
       const bool is_inlet = (type == 2 || type == 4);
       const int gi = is_inlet ? ioid : a.n_in + ioid;
       const int model = is_inlet ? a.inlet_model : a.outlet_model;
@@ -139,11 +140,11 @@ struct BoundaryAll {
                                       block_xyz[3 * b] * 8 + x, block_xyz[3 * b + 1] * 8 + y,
                                       block_xyz[3 * b + 2] * 8 + z);
       Store<P>::store(fn + own, inv * kSites + l, v, a);
-    } else if (D > 0 && (type == 1 || type == 4 || type == 5) && ((wm >> (D - 1)) & 1u)) {
+    } else if (D > 0 && (type == 1 || type == 4 || type == 5) && ((wm >> db) & 1u)) {
       T v = fpost[D];
       if (a.wall == 1) {
         const T q = (T)a.b_cut[r * (Q - 1) + D - 1];
-        if (!(((wm >> (inv - 1)) & 1u) || q < (T)0.5))
+        if (!(((wm >> ib) & 1u) || q < (T)0.5))
           v = (fpost[D] + ((T)2.0 * q - (T)1) * fpost[inv]) / ((T)2.0 * q);
       }
       Store<P>::store(fn + own, inv * kSites + l, v, a);
@@ -533,7 +534,7 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
 
 template <int P, int THREADS, int MINB, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArgs a, const int32_t* block_xyz) {
-  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  MonAcc acc = mon_neutral();
   bool check = false;
   if constexpr (MON) check = *a.mon_state != 0;
   collide_listed_warp<P, MON>(a, ((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5, block_xyz, acc, check);
@@ -564,7 +565,7 @@ void launch_listed(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
 template <int P, int THREADS, int MINB, bool PERSIST, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_stream_collide(StepArgs a, const int32_t* block_xyz) {
-  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  MonAcc acc = mon_neutral();
   bool check = false;
   if constexpr (MON) check = *a.mon_state != 0;
   if constexpr (!PERSIST) {
@@ -594,7 +595,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
 static __global__ void __launch_bounds__(256) k_mon_stage2(const double* __restrict__ in, int64_t n_in,
                                                            int64_t per, double* __restrict__ out,
                                                            int64_t n_out) {
-  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  MonAcc acc = mon_neutral();
   const int64_t lo = (int64_t)blockIdx.x * per, hi = lo + per < n_in ? lo + per : n_in;
   for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
     mon_combine(acc, MonAcc{in[i], in[n_in + i], in[2 * n_in + i], (unsigned long long)in[3 * n_in + i],
@@ -620,7 +621,7 @@ static __global__ void __launch_bounds__(256) k_mon_stage2(const double* __restr
 static __global__ void __launch_bounds__(256) k_mon_final(const double* __restrict__ part, int64_t n,
                                                           int32_t* mon_state, double* result,
                                                           SteadyArgs sa, int steady) {
-  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  MonAcc acc = mon_neutral();
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
     mon_combine(acc, MonAcc{part[i], part[n + i], part[2 * n + i], (unsigned long long)part[3 * n + i],
                             part[4 * n + i], part[5 * n + i], part[6 * n + i]});
@@ -876,7 +877,7 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
   StepArgs a{};
   a.fp16_scale = ma.fp16_scale;
   a.fp16_inv_scale = ma.fp16_inv_scale;
-  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  MonAcc acc = mon_neutral();
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t code = (s < ma.nslot) ? (ma.block_bulk[s >> 9] ? 1u : ma.site_code[s]) : 0u;
   if (code != 0) {
@@ -945,7 +946,7 @@ __global__ void __launch_bounds__(256) k_monitor(MonitorArgs ma) {
 // Reduce the per-CTA partials of k_monitor in a fixed order into element 0 of
 // each partial array (one CTA of 256 threads; thread t folds partials t, t+256, ...).
 static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, int64_t nparts) {
-  MonAcc acc{0.0, 0.0, 1.0e300, 0ull};
+  MonAcc acc = mon_neutral();
   for (int64_t i = threadIdx.x; i < nparts; i += blockDim.x)
     mon_combine(acc, MonAcc{ma.part_mass[i], ma.part_max[i], ma.part_min[i], ma.part_bad[i], 1.0e300, -1.0e300,
                             0.0});
