@@ -474,12 +474,15 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
   }
 }
 
+// Element stride between directions of one thread in the staged launch's buffer.
+constexpr int kStageStride = 128;
+
 // One warp of the fluid list: 32 fluid sites of one block (or the zero-fill of its
 // solid slots that share sectors with fluid), so no lane is spent on a solid slot.
-template <int P, bool MON>
+template <int P, bool MON, bool STAGED = false>
 __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w,
                                                     const int32_t* __restrict__ block_xyz, MonAcc& acc,
-                                                    bool check) {
+                                                    bool check, const float* staged = nullptr) {
   using St = Store<P>;
   using S = typename St::S;
   using T = typename Calc<P>::T;
@@ -507,8 +510,13 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + j;
   T f[Q], fpost[Q];
   if (code != 0) {
+    if constexpr (STAGED) {
 #pragma unroll
-    for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
+      for (int i = 0; i < Q; ++i) f[i] = staged[i * kStageStride];
+    } else {
+#pragma unroll
+      for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
+    }
   } else {
 #pragma unroll
     for (int i = 0; i < Q; ++i) f[i] = (T)(P == 0 ? weight_d(i) : 0.0);
@@ -530,6 +538,61 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
     PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, j, b * (Q * kSites), code != 0, false, links,
                          r, type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
   }
+}
+
+// Staged fluid-list launch (FP32 deviations): a persistent grid whose warps walk
+// the fluid list with a stride; while a warp collides one unit, the 19 values of
+// each lane of its next unit are already on their way into shared memory
+// (cp.async, 4 bytes per lane and direction, lane-private), so loads stay in flight
+// without holding registers.  Shared memory: 2 stages x 19 x (THREADS) floats.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_none() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int THREADS>
+__device__ __forceinline__ void stage_unit(const StepArgs& a, int64_t u, float* dst) {
+  if (u >= a.n_warps) return;
+  const int32_t e = __ldg(a.warp_block + u);
+  if (e < 0) return;  // a zero-fill warp reads nothing
+  const unsigned js = __ldg(a.lane_slot + u * 32 + (threadIdx.x & 31));
+  if (js == 0xffffu) return;
+  const float* src = static_cast<const float*>(a.f_old) + (int64_t)e * (Q * kSites) + js;
+#pragma unroll
+  for (int d = 0; d < Q; ++d) cp_async4(dst + d * kStageStride, src + d * kSites);
+}
+
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_staged(StepArgs a, const int32_t* block_xyz) {
+  static_assert(THREADS == kStageStride, "stage layout");
+  __shared__ float buf[2][Q * THREADS];  // [stage][d * THREADS + thread]
+  MonAcc acc = mon_neutral();
+  const int64_t stride = (int64_t)gridDim.x * (THREADS / 32);
+  int64_t u = (int64_t)blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5);
+  stage_unit<THREADS>(a, u, &buf[0][threadIdx.x]);
+  cp_async_commit();
+  int st = 0;
+  for (; u < a.n_warps; u += stride, st ^= 1) {
+    stage_unit<THREADS>(a, u + stride, &buf[st ^ 1][threadIdx.x]);
+    cp_async_commit();
+    cp_async_wait_one();  // this lane's copies of unit u have landed
+    collide_listed_warp<1, false, true>(a, u, block_xyz, acc, false, &buf[st][threadIdx.x]);
+  }
+  cp_async_wait_none();
+}
+
+template <int THREADS, int MINB>
+void launch_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream_collide_staged<THREADS, MINB>, THREADS, 0);
+  const int64_t need = (a.n_warps * 32 + THREADS - 1) / THREADS;
+  const int64_t g = std::min<int64_t>(need, (int64_t)sms * std::max(per_sm, 1));
+  if (g > 0) k_stream_collide_staged<THREADS, MINB><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
 }
 
 template <int P, int THREADS, int MINB, bool MON>
@@ -1019,6 +1082,13 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       launch_listed<P, 128, (P == 0 ? 2 : 10), false>(a, bxyz, st);                             \
       return;                                                                                   \
     }                                                                                           \
+    if (variant == 7) {                                                                         \
+      if (P == 1 && !a.mon_u) {                                                                 \
+        launch_staged<128, 8>(a, bxyz, st);                                                     \
+        return;                                                                                 \
+      }                                                                                         \
+      variant = 6; /* staged only for unmonitored FP32 deviations */                            \
+    }                                                                                           \
     if (variant == 6) {                                                                         \
       if (a.mon_u) launch_listed<P, 128, (P == 0 ? 2 : 8), true>(a, bxyz, st);                  \
       else launch_listed<P, 128, (P == 0 ? 2 : 8), false>(a, bxyz, st);                         \
@@ -1044,7 +1114,7 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     }                                                                                           \
   }                                                                                             \
   int64_t monitored_grid_##P(int64_t nslot, int variant, int64_t n_warps) {                    \
-    if (variant == 5 || variant == 6) return (n_warps * 32 + 127) / 128;                        \
+    if (variant >= 5) return (n_warps * 32 + 127) / 128; /* monitored 7 runs as 6 */            \
     if (P == 0) return nslot / 128;                                                             \
     switch (variant) {                                                                          \
       case 1: return nslot / 128;                                                               \

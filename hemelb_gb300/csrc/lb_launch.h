@@ -12,7 +12,7 @@ struct StepArgs;
 // Launch variants of the stream-and-collide kernel (FP32 / FP16 forms; FP64 has one):
 // 0 default shape, 1: 128x8, 2: 256x4, 3: 512x2 threads x resident CTAs per SM,
 // 4: persistent 128-thread CTAs striding over the slots.
-constexpr int kSCVariants = 7;  // 5, 6: the fluid-list launch
+constexpr int kSCVariants = 8;  // 5, 6: the fluid-list launch; 7: staged (FP32)
 
 struct PostArgs {
   void* f_new;
