@@ -540,11 +540,11 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   }
 }
 
-// Staged fluid-list launch (FP32 deviations): a persistent grid whose warps walk
-// the fluid list with a stride; while a warp collides one unit, the 19 values of
-// each lane of its next unit are already on their way into shared memory
-// (cp.async, 4 bytes per lane and direction, lane-private), so loads stay in flight
-// without holding registers.  Shared memory: 2 stages x 19 x (THREADS) floats.
+// Staged fluid-list launch (FP32 deviations): each warp takes a few consecutive
+// units of the fluid list; while it collides one unit, the 19 values of each lane
+// of its next unit are already on their way into shared memory (cp.async, 4 bytes
+// per lane and direction, lane-private), so loads stay in flight without holding
+// registers.  Shared memory: 2 stages x 19 x THREADS floats.
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
@@ -565,34 +565,32 @@ __device__ __forceinline__ void stage_unit(const StepArgs& a, int64_t u, float* 
   for (int d = 0; d < Q; ++d) cp_async4(dst + d * kStageStride, src + d * kSites);
 }
 
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int UNITS>
 __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_staged(StepArgs a, const int32_t* block_xyz) {
   static_assert(THREADS == kStageStride, "stage layout");
   __shared__ float buf[2][Q * THREADS];  // [stage][d * THREADS + thread]
   MonAcc acc = mon_neutral();
-  const int64_t stride = (int64_t)gridDim.x * (THREADS / 32);
-  int64_t u = (int64_t)blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5);
-  stage_unit<THREADS>(a, u, &buf[0][threadIdx.x]);
+  // this warp's UNITS consecutive units of the fluid list (launch order keeps
+  // neighbouring blocks close in time, so their shared sectors merge in L2)
+  const int64_t u0 = ((int64_t)blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5)) * UNITS;
+  stage_unit<THREADS>(a, u0, &buf[0][threadIdx.x]);
   cp_async_commit();
-  int st = 0;
-  for (; u < a.n_warps; u += stride, st ^= 1) {
-    stage_unit<THREADS>(a, u + stride, &buf[st ^ 1][threadIdx.x]);
+#pragma unroll 1
+  for (int k = 0; k < UNITS; ++k) {
+    const int st = k & 1;
+    if (k + 1 < UNITS) stage_unit<THREADS>(a, u0 + k + 1, &buf[st ^ 1][threadIdx.x]);
     cp_async_commit();
-    cp_async_wait_one();  // this lane's copies of unit u have landed
-    collide_listed_warp<1, false, true>(a, u, block_xyz, acc, false, &buf[st][threadIdx.x]);
+    cp_async_wait_one();  // this lane's copies of unit u0 + k have landed
+    collide_listed_warp<1, false, true>(a, u0 + k, block_xyz, acc, false, &buf[st][threadIdx.x]);
   }
   cp_async_wait_none();
 }
 
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int UNITS>
 void launch_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream_collide_staged<THREADS, MINB>, THREADS, 0);
-  const int64_t need = (a.n_warps * 32 + THREADS - 1) / THREADS;
-  const int64_t g = std::min<int64_t>(need, (int64_t)sms * std::max(per_sm, 1));
-  if (g > 0) k_stream_collide_staged<THREADS, MINB><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
+  const int64_t per_cta = (THREADS / 32) * UNITS;
+  const int64_t g = (a.n_warps + per_cta - 1) / per_cta;
+  if (g > 0) k_stream_collide_staged<THREADS, MINB, UNITS><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
 }
 
 template <int P, int THREADS, int MINB, bool MON>
@@ -1084,7 +1082,7 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     }                                                                                           \
     if (variant == 7) {                                                                         \
       if (P == 1 && !a.mon_u) {                                                                 \
-        launch_staged<128, 8>(a, bxyz, st);                                                     \
+        launch_staged<128, 8, 4>(a, bxyz, st);                                                  \
         return;                                                                                 \
       }                                                                                         \
       variant = 6; /* staged only for unmonitored FP32 deviations */                            \
