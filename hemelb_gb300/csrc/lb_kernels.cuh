@@ -6,6 +6,7 @@
 #include "lb_launch.h"
 
 #include <algorithm>
+#include <type_traits>
 
 // Launch shape of the stream-and-collide kernel (threads per CTA must divide 512;
 // minimum resident CTAs per SM for the FP32 / FP16 forms and for FP64).
@@ -327,6 +328,61 @@ __device__ __forceinline__ MonAcc mon_block(MonAcc v) {
   return v;
 }
 
+// The FP32 forms accumulate their per-thread monitor values in FP32 (min / max are
+// exact in any precision; the mass as a count plus the sum of the density
+// deviations, which are small) and switch to FP64 only for each warp's result:
+// GB300's FP64 rate would otherwise make every monitored site an FP64 workload.
+struct MonAccF {
+  float dm, maxdu, minf, dmin, dmax, umax;  // dm: sum of rho - 1; dmin/dmax: of rho - 1
+  unsigned count, bad;
+};
+__device__ __forceinline__ MonAccF mon_neutral_f() {
+  return MonAccF{0.f, 0.f, 1.0e30f, 1.0e30f, -1.0e30f, 0.f, 0u, 0u};
+}
+__device__ __forceinline__ void mon_combine_f(MonAccF& a, const MonAccF& b) {
+  a.dm += b.dm;
+  if (!(b.maxdu <= a.maxdu)) a.maxdu = b.maxdu;
+  a.minf = fminf(a.minf, b.minf);
+  a.dmin = fminf(a.dmin, b.dmin);
+  a.dmax = fmaxf(a.dmax, b.dmax);
+  if (!(b.umax <= a.umax)) a.umax = b.umax;
+  a.count += b.count;
+  a.bad += b.bad;
+}
+// CTA-wide: FP32 within each warp, FP64 across the warps' results; valid in thread 0.
+__device__ __forceinline__ MonAcc mon_block_f(MonAccF v) {
+  for (int off = 16; off > 0; off >>= 1) {
+    MonAccF o;
+    o.dm = __shfl_down_sync(0xffffffffu, v.dm, off);
+    o.maxdu = __shfl_down_sync(0xffffffffu, v.maxdu, off);
+    o.minf = __shfl_down_sync(0xffffffffu, v.minf, off);
+    o.dmin = __shfl_down_sync(0xffffffffu, v.dmin, off);
+    o.dmax = __shfl_down_sync(0xffffffffu, v.dmax, off);
+    o.umax = __shfl_down_sync(0xffffffffu, v.umax, off);
+    o.count = __shfl_down_sync(0xffffffffu, v.count, off);
+    o.bad = __shfl_down_sync(0xffffffffu, v.bad, off);
+    mon_combine_f(v, o);
+  }
+  MonAcc d = mon_neutral();
+  if (v.count) {
+    d.mass = (double)v.count + (double)v.dm;
+    d.maxdu = (double)v.maxdu;
+    d.minf = (double)v.minf;
+    d.bad = v.bad;
+    d.rmin = 1.0 + (double)v.dmin;
+    d.rmax = 1.0 + (double)v.dmax;
+    d.umax = (double)v.umax;
+  }
+  __shared__ MonAcc sh[32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh[w] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) mon_combine(d, sh[k]);
+  }
+  return d;
+}
+
 // Fused StabilityTester for one fluid site of a monitored step
 // (Code/lb/StabilityTester.h:91-183): the velocity of the state being collided,
 // m / rho with the moments of the collision (the reference's
@@ -334,64 +390,79 @@ __device__ __forceinline__ MonAcc mon_block(MonAcc v) {
 // updated; f > 0 over all directions; the density for the mass.  The new velocity
 // is recorded for the next step.
 template <int P>
-__device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const typename Calc<P>::T* f,
-                                         typename Calc<P>::T m0, typename Calc<P>::T mx,
-                                         typename Calc<P>::T my, typename Calc<P>::T mz, MonAcc& acc,
-                                         bool check) {
+__device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const double* f, double m0, double mx,
+                                         double my, double mz, MonAcc& acc, bool check) {
+  // FP64 form: the reference's arithmetic (m / rho, |du| by inner product)
   const int64_t ui = (s >> 9) * (3 * kSites) + (s & (kSites - 1));
-  if constexpr (P == 0) {
-    double* u = static_cast<double*>(a.mon_u);
-    const double ux = mx / m0, uy = my / m0, uz = mz / m0;
-    if (check) {
-      const double dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
-      const double du = sqrt(dot3d(dx, dy, dz, dx, dy, dz));
-      if (!(du <= acc.maxdu)) acc.maxdu = du;
-      acc.mass += m0;
-      acc.rmin = fmin(acc.rmin, m0);
-      acc.rmax = fmax(acc.rmax, m0);
-      const double um = sqrt(dot3d(ux, uy, uz, ux, uy, uz));
-      if (!(um <= acc.umax)) acc.umax = um;
-      bool bad = false;
-      double mn = f[0];
+  double* u = static_cast<double*>(a.mon_u);
+  const double ux = mx / m0, uy = my / m0, uz = mz / m0;
+  if (check) {
+    const double dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
+    const double du = sqrt(dot3d(dx, dy, dz, dx, dy, dz));
+    if (!(du <= acc.maxdu)) acc.maxdu = du;
+    acc.mass += m0;
+    acc.rmin = fmin(acc.rmin, m0);
+    acc.rmax = fmax(acc.rmax, m0);
+    const double um = sqrt(dot3d(ux, uy, uz, ux, uy, uz));
+    if (!(um <= acc.umax)) acc.umax = um;
+    bool bad = false;
+    double mn = f[0];
 #pragma unroll
-      for (int d = 0; d < Q; ++d) {
-        bad |= !(f[d] > 0.0);
-        mn = fmin(mn, f[d]);
-      }
-      acc.minf = fmin(acc.minf, mn);
-      acc.bad += bad ? 1ull : 0ull;
+    for (int d = 0; d < Q; ++d) {
+      bad |= !(f[d] > 0.0);
+      mn = fmin(mn, f[d]);
     }
-    u[ui] = ux;
-    u[ui + kSites] = uy;
-    u[ui + 2 * kSites] = uz;
-  } else {
-    float* u = static_cast<float*>(a.mon_u);
-    const float ir = 1.f / (1.f + m0);
-    const float ux = mx * ir, uy = my * ir, uz = mz * ir;
-    if (check) {
-      const float dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
-      const double du = (double)sqrtf(dx * dx + dy * dy + dz * dz);
-      if (!(du <= acc.maxdu)) acc.maxdu = du;
-      acc.mass += 1.0 + (double)m0;
-      acc.rmin = fmin(acc.rmin, 1.0 + (double)m0);
-      acc.rmax = fmax(acc.rmax, 1.0 + (double)m0);
-      const double um = (double)sqrtf(ux * ux + uy * uy + uz * uz);
-      if (!(um <= acc.umax)) acc.umax = um;
-      bool bad = false;
-      float mn = 1.0e30f;
-#pragma unroll
-      for (int d = 0; d < Q; ++d) {
-        const float fv = f[d] + weight_f(d);
-        bad |= !(fv > 0.f);
-        mn = fminf(mn, fv);
-      }
-      acc.minf = fmin(acc.minf, (double)mn);
-      acc.bad += bad ? 1ull : 0ull;
-    }
-    u[ui] = ux;
-    u[ui + kSites] = uy;
-    u[ui + 2 * kSites] = uz;
+    acc.minf = fmin(acc.minf, mn);
+    acc.bad += bad ? 1ull : 0ull;
   }
+  u[ui] = ux;
+  u[ui + kSites] = uy;
+  u[ui + 2 * kSites] = uz;
+}
+
+template <int P>
+__device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const float* f, float m0, float mx,
+                                         float my, float mz, MonAccF& acc, bool check) {
+  // deviation forms: m0 = rho - 1
+  const int64_t ui = (s >> 9) * (3 * kSites) + (s & (kSites - 1));
+  float* u = static_cast<float*>(a.mon_u);
+  const float ir = 1.f / (1.f + m0);
+  const float ux = mx * ir, uy = my * ir, uz = mz * ir;
+  if (check) {
+    const float dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
+    const float du = sqrtf(dx * dx + dy * dy + dz * dz);
+    if (!(du <= acc.maxdu)) acc.maxdu = du;
+    acc.dm += m0;
+    acc.dmin = fminf(acc.dmin, m0);
+    acc.dmax = fmaxf(acc.dmax, m0);
+    const float um = sqrtf(ux * ux + uy * uy + uz * uz);
+    if (!(um <= acc.umax)) acc.umax = um;
+    bool bad = false;
+    float mn = 1.0e30f;
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      const float fv = f[d] + weight_f(d);
+      bad |= !(fv > 0.f);
+      mn = fminf(mn, fv);
+    }
+    acc.minf = fminf(acc.minf, mn);
+    acc.bad += bad ? 1u : 0u;
+    acc.count += 1u;
+  }
+  u[ui] = ux;
+  u[ui + kSites] = uy;
+  u[ui + 2 * kSites] = uz;
+}
+
+template <int P>
+using MonAccT = typename std::conditional<P == 0, MonAcc, MonAccF>::type;
+template <int P>
+__device__ __forceinline__ MonAccT<P> mon_neutral_t() {
+  if constexpr (P == 0) return mon_neutral(); else return mon_neutral_f();
+}
+template <int P>
+__device__ __forceinline__ MonAcc mon_block_t(const MonAccT<P>& v) {
+  if constexpr (P == 0) return mon_block(v); else return mon_block_f(v);
 }
 
 // ---------------------------------------------------------------------------
@@ -428,7 +499,7 @@ __device__ __forceinline__ void site_update(const StepArgs& a, const B& base,
 // every lane of a warp with any fluid site stays converged through the pushes.
 template <int P, bool MON>
 __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
-                                             const int32_t* __restrict__ block_xyz, MonAcc& acc,
+                                             const int32_t* __restrict__ block_xyz, MonAccT<P>& acc,
                                              bool check) {
   using St = Store<P>;
   using S = typename St::S;
@@ -481,7 +552,7 @@ constexpr int kStageStride = 128;
 // solid slots that share sectors with fluid), so no lane is spent on a solid slot.
 template <int P, bool MON, bool STAGED = false>
 __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w,
-                                                    const int32_t* __restrict__ block_xyz, MonAcc& acc,
+                                                    const int32_t* __restrict__ block_xyz, MonAccT<P>& acc,
                                                     bool check, const float* staged = nullptr) {
   using St = Store<P>;
   using S = typename St::S;
@@ -569,7 +640,7 @@ template <int THREADS, int MINB, int UNITS>
 __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_staged(StepArgs a, const int32_t* block_xyz) {
   static_assert(THREADS == kStageStride, "stage layout");
   __shared__ float buf[2][Q * THREADS];  // [stage][d * THREADS + thread]
-  MonAcc acc = mon_neutral();
+  MonAccF acc = mon_neutral_f();  // unused: the staged launch is not monitored
   // this warp's UNITS consecutive units of the fluid list (launch order keeps
   // neighbouring blocks close in time, so their shared sectors merge in L2)
   const int64_t u0 = ((int64_t)blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5)) * UNITS;
@@ -595,21 +666,21 @@ void launch_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
 
 template <int P, int THREADS, int MINB, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArgs a, const int32_t* block_xyz) {
-  MonAcc acc = mon_neutral();
+  MonAccT<P> acc = mon_neutral_t<P>();
   bool check = false;
   if constexpr (MON) check = *a.mon_state != 0;
   collide_listed_warp<P, MON>(a, ((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5, block_xyz, acc, check);
   if constexpr (MON) {
-    acc = mon_block(acc);
+    const MonAcc r = mon_block_t<P>(acc);
     if (threadIdx.x == 0) {
       const int64_t n = a.mon_nparts;
-      a.mon_part[blockIdx.x] = acc.mass;
-      a.mon_part[n + blockIdx.x] = acc.maxdu;
-      a.mon_part[2 * n + blockIdx.x] = acc.minf;
-      a.mon_part[3 * n + blockIdx.x] = (double)acc.bad;
-      a.mon_part[4 * n + blockIdx.x] = acc.rmin;
-      a.mon_part[5 * n + blockIdx.x] = acc.rmax;
-      a.mon_part[6 * n + blockIdx.x] = acc.umax;
+      a.mon_part[blockIdx.x] = r.mass;
+      a.mon_part[n + blockIdx.x] = r.maxdu;
+      a.mon_part[2 * n + blockIdx.x] = r.minf;
+      a.mon_part[3 * n + blockIdx.x] = (double)r.bad;
+      a.mon_part[4 * n + blockIdx.x] = r.rmin;
+      a.mon_part[5 * n + blockIdx.x] = r.rmax;
+      a.mon_part[6 * n + blockIdx.x] = r.umax;
     }
   }
 }
@@ -626,7 +697,7 @@ void launch_listed(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
 template <int P, int THREADS, int MINB, bool PERSIST, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_stream_collide(StepArgs a, const int32_t* block_xyz) {
-  MonAcc acc = mon_neutral();
+  MonAccT<P> acc = mon_neutral_t<P>();
   bool check = false;
   if constexpr (MON) check = *a.mon_state != 0;
   if constexpr (!PERSIST) {
@@ -637,16 +708,16 @@ __global__ void __launch_bounds__(THREADS, MINB)
       collide_slot<P, MON>(a, c * THREADS + threadIdx.x, block_xyz, acc, check);
   }
   if constexpr (MON) {
-    acc = mon_block(acc);
+    const MonAcc r = mon_block_t<P>(acc);
     if (threadIdx.x == 0) {
       const int64_t n = a.mon_nparts;
-      a.mon_part[blockIdx.x] = acc.mass;
-      a.mon_part[n + blockIdx.x] = acc.maxdu;
-      a.mon_part[2 * n + blockIdx.x] = acc.minf;
-      a.mon_part[3 * n + blockIdx.x] = (double)acc.bad;
-      a.mon_part[4 * n + blockIdx.x] = acc.rmin;
-      a.mon_part[5 * n + blockIdx.x] = acc.rmax;
-      a.mon_part[6 * n + blockIdx.x] = acc.umax;
+      a.mon_part[blockIdx.x] = r.mass;
+      a.mon_part[n + blockIdx.x] = r.maxdu;
+      a.mon_part[2 * n + blockIdx.x] = r.minf;
+      a.mon_part[3 * n + blockIdx.x] = (double)r.bad;
+      a.mon_part[4 * n + blockIdx.x] = r.rmin;
+      a.mon_part[5 * n + blockIdx.x] = r.rmax;
+      a.mon_part[6 * n + blockIdx.x] = r.umax;
     }
   }
 }
