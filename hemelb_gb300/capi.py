@@ -112,6 +112,7 @@ SIGNATURES = {
     "hlbg_set_launch_variant": (C.c_int, [C.c_void_p, C.c_int32]),
     "hlbg_step_monitored": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Stats)]),
     "hlbg_incompressibility": (C.c_int, [C.c_void_p, C.POINTER(Incomp)]),
+    "hlbg_wall_shear_stress": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_set_block_tau": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_stream_and_collide_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
     "hlbg_post_step_range": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),

@@ -113,6 +113,8 @@ struct hlbg_ctx {
   int8_t* d_b_type = nullptr;
   float* d_b_cut = nullptr;
   uint64_t* d_b_links = nullptr;  // 3-bit link code per direction (see lb_device.cuh)
+  float* d_b_normal = nullptr;      // wall normal per record
+  double* d_wss = nullptr;          // wall shear stress output, allocated on first use
   int32_t* d_rec_slot = nullptr;  // slot of each record
   std::vector<int32_t> h_new_of_old;  // device block index of each input block
   double* d_blk_omega = nullptr;      // optional per-block (omega+, omega-)
@@ -438,6 +440,7 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   std::vector<int32_t> rid;
   std::vector<int8_t> rtype, stype;
   std::vector<float> rcut;
+  std::vector<float> rnorm;
   const bool want_cut = ctx->params.wall == HLBG_WALL_BFL;
   if (want_cut && !g->cut_distance && nin > 0)
     return fail(ctx, HLBG_ERR_INVAL, "BFL walls need cut distances");
@@ -472,6 +475,23 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     rw.push_back(wm);
     ri.push_back(im);
     rid.push_back(io);
+    {  // wall normal: the geometry's, else the normalised sum of the wall-link vectors
+      double n[3] = {0.0, 0.0, 0.0};
+      if (ir >= 0 && g->wall_normal) {
+        for (int c = 0; c < 3; ++c) n[c] = g->wall_normal[ir * 3 + c];
+      } else {
+        for (int d = 1; d < 19; ++d)
+          if ((wm >> (d - 1)) & 1u) {
+            n[0] += HCX[d];
+            n[1] += HCY[d];
+            n[2] += HCZ[d];
+          }
+        const double m = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (m > 0)
+          for (auto& c : n) c /= m;
+      }
+      for (double c : n) rnorm.push_back((float)c);
+    }
     rtype.push_back((int8_t)ct);
     site_ctype[s] = (int8_t)ct;
     if (want_cut)
@@ -635,6 +655,7 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   if ((rc = upload(ctx, &ctx->d_b_type, rtype))) return rc;
   if (want_cut && (rc = upload(ctx, &ctx->d_b_cut, rcut))) return rc;
   if ((rc = upload(ctx, &ctx->d_b_links, rlinks))) return rc;
+  if ((rc = upload(ctx, &ctx->d_b_normal, rnorm))) return rc;
   if ((rc = upload(ctx, &ctx->d_rec_slot, ctx->h_rec_slot))) return rc;
   {
     std::vector<int32_t> io_rec;
@@ -822,7 +843,7 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_list,      ctx->d_part,      ctx->d_part_bad,  ctx->d_steady,
                   ctx->d_steady_n,  ctx->d_slot2site, ctx->d_site2slot, ctx->d_mon_u,
                   ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result,
-                  ctx->d_warp_block, ctx->d_lane_slot};
+                  ctx->d_warp_block, ctx->d_lane_slot, ctx->d_b_normal, ctx->d_wss};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
@@ -1187,6 +1208,36 @@ int hlbg_step_monitored(hlbg_ctx* ctx, int32_t nsteps, hlbg_stats* out) {
   out->unstable_sites = valid ? (int64_t)r[3] : 0;
   out->time_step = valid ? (int64_t)ctx->t1 - 1 : -1;
   return valid && r[3] > 0.0 ? HLBG_ERR_UNSTABLE : HLBG_OK;
+}
+
+int hlbg_wall_shear_stress(hlbg_ctx* ctx, double* out) {
+  if (!ctx || !out) return HLBG_ERR_INVAL;
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  if (!ctx->d_wss) {
+    int rc = dev_alloc(ctx, &ctx->d_wss, (size_t)ctx->nsites);
+    if (rc) return rc;
+  }
+  WssArgs wa{};
+  wa.f = ctx->f[ctx->cur];
+  wa.ref2slot = ctx->d_ref2slot;
+  wa.site_code = ctx->d_site_code;
+  wa.block_bulk = ctx->d_block_bulk;
+  wa.b_wall = ctx->d_b_wall;
+  wa.b_normal = ctx->d_b_normal;
+  // LbmParameters::CalcDerivedParams (Code/lb/LbmParameters.h:37)
+  wa.stress_param = (1.0 - 1.0 / (2.0 * ctx->params.tau)) / std::sqrt(2.0);
+  wa.count = ctx->nsites;
+  wa.out = ctx->d_wss;
+  wa.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+  switch (ctx->prec) {
+    case 0: launch_wss_0(wa, ctx->stream); break;
+    case 1: launch_wss_1(wa, ctx->stream); break;
+    default: launch_wss_2(wa, ctx->stream); break;
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, ctx->d_wss, sizeof(double) * ctx->nsites, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return HLBG_OK;
 }
 
 int hlbg_incompressibility(hlbg_ctx* ctx, hlbg_incomp* out) {

@@ -1092,6 +1092,77 @@ static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, in
   }
 }
 
+// Lattice::CalculateWallShearStressMagnitude (Code/lb/lattices/Lattice.h:652-686)
+// with CalculatePiTensor (:696-726) on f_neq = f - f_eq of the state, as
+// UpdateCachePostCollision fills wallShearStressMagnitudeCache
+// (Code/lb/streamers/Common.h:35-52): FP64 and the reference's operation order.
+template <int P>
+__global__ void k_wss(WssArgs wa) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= wa.count) return;
+  const int64_t s = wa.ref2slot[i];
+  const uint32_t code = wa.block_bulk[s >> 9] ? 1u : wa.site_code[s];
+  const uint32_t wm = code >= 2 ? wa.b_wall[code - 2] : 0u;
+  if (wm == 0) {  // site.IsWall() is false: NO_VALUE
+    wa.out[i] = 1.7976931348623157e308;
+    return;
+  }
+  double f[Q];
+  const int64_t off = fidx(s, 0);
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    if constexpr (P == 0) {
+      f[d] = static_cast<const double*>(wa.f)[off + d * kSites];
+    } else if constexpr (P == 1) {
+      f[d] = (double)static_cast<const float*>(wa.f)[off + d * kSites] + weight_d(d);
+    } else {
+      f[d] = (double)(__half2float(static_cast<const __half*>(wa.f)[off + d * kSites]) * wa.fp16_inv_scale) +
+             weight_d(d);
+    }
+  }
+  double rho = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    rho += f[d];
+    mx += (double)Lat::cx(d) * f[d];
+    my += (double)Lat::cy(d) * f[d];
+    mz += (double)Lat::cz(d) * f[d];
+  }
+  double feq[Q];
+  feq64(rho, mx, my, mz, feq);
+  double fneq[Q];
+#pragma unroll
+  for (int d = 0; d < Q; ++d) fneq[d] = f[d] - feq[d];
+  double pi[3][3];
+#pragma unroll
+  for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+    for (int jj = 0; jj <= ii; ++jj) {
+      double acc = 0.0;
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        const double ci = ii == 0 ? (double)Lat::cx(d) : (ii == 1 ? (double)Lat::cy(d) : (double)Lat::cz(d));
+        const double cj = jj == 0 ? (double)Lat::cx(d) : (jj == 1 ? (double)Lat::cy(d) : (double)Lat::cz(d));
+        acc += fneq[d] * ci * cj;
+      }
+      pi[ii][jj] = acc;
+      pi[jj][ii] = acc;
+    }
+  const double nor[3] = {(double)wa.b_normal[3 * (code - 2)], (double)wa.b_normal[3 * (code - 2) + 1],
+                         (double)wa.b_normal[3 * (code - 2) + 2]};
+  const double temp = wa.stress_param * (-sqrt(2.0));
+  double sq = 0.0, nrm = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    double sv = 0.0;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) sv += pi[a][b] * nor[b] * temp;
+    sq += sv * sv;
+    nrm += sv * nor[a];
+  }
+  wa.out[i] = sqrt(sq - nrm * nrm);
+}
+
 // Mean of the two time levels on every fluid slot (the arrays hold consecutive
 // states right after a step): removes the period-two component of the state.
 template <int P>
@@ -1233,6 +1304,10 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     const int64_t nparts = (ma.nslot + 255) / 256;                                              \
     k_monitor<P><<<(unsigned)nparts, 256, 0, st>>>(ma);                                         \
     k_monitor_final<<<1, 256, 0, st>>>(ma, nparts);                                             \
+  }                                                                                             \
+  void launch_wss_##P(const WssArgs& wa, cudaStream_t st) {                                     \
+    unsigned g = (unsigned)((wa.count + 255) / 256);                                            \
+    if (g) k_wss<P><<<g, 256, 0, st>>>(wa);                                                     \
   }                                                                                             \
   void launch_average_##P(const AverageArgs& aa, cudaStream_t st) {                             \
     unsigned g = (unsigned)((aa.nslot + 255) / 256);                                            \

@@ -90,6 +90,21 @@ struct AverageArgs {
   float fp16_scale, fp16_inv_scale;
 };
 
+// Wall shear stress magnitude per site in contiguous order (DBL_MAX where the
+// site has no wall link), for the state in f.
+struct WssArgs {
+  const void* f;
+  const int32_t* ref2slot;
+  const uint32_t* site_code;
+  const uint8_t* block_bulk;
+  const uint32_t* b_wall;
+  const float* b_normal;  // [nrec * 3]
+  double stress_param;
+  int64_t count;
+  double* out;
+  float fp16_inv_scale;
+};
+
 #define HLBG_DECLARE(P)                                                              \
   void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st,  \
                                  int variant);                                           \
@@ -106,7 +121,8 @@ struct AverageArgs {
   void launch_mon_reduce_##P(const double* part, int64_t nparts, double* part2, int64_t n2,    \
                              int32_t* mon_state, double* result, const SteadyArgs& sa,        \
                              int steady, cudaStream_t st);                                     \
-  void launch_average_##P(const AverageArgs& aa, cudaStream_t st);
+  void launch_average_##P(const AverageArgs& aa, cudaStream_t st);                    \
+  void launch_wss_##P(const WssArgs& wa, cudaStream_t st);
 
 HLBG_DECLARE(0)
 HLBG_DECLARE(1)

@@ -102,6 +102,32 @@ bool inside_shape(const Shape& s, Vec p) {
   return dx * dx + dy * dy < rr * rr;
 }
 
+// Signed distance of p inside shape s (positive inside) and the outward unit
+// gradient of that distance's complement (the wall normal pointing out of the
+// fluid); false where the gradient is undefined (on the axis).
+bool shape_normal(const Shape& s, Vec p, double& sd, Vec& n) {
+  if (s.kind == 0) {
+    const Vec v = sub(s.b, s.a), w = sub(p, s.a);
+    double t = dot(w, v) / dot(v, v);
+    t = std::min(1.0, std::max(0.0, t));
+    const Vec c = sub(w, mul(v, t));
+    const double d = std::sqrt(dot(c, c));
+    sd = s.r - d;
+    if (d < 1e-12) return false;
+    n = mul(c, 1.0 / d);
+    return true;
+  }
+  const double dz = p.z - s.zc;
+  const double g = std::exp(-dz * dz / (2.0 * s.sigma * s.sigma));
+  const double R = s.r * (1.0 - s.depth * g);
+  const double dRdz = s.r * s.depth * g * dz / (s.sigma * s.sigma);
+  const double dx = p.x - s.a.x, dy = p.y - s.a.y, rho = std::sqrt(dx * dx + dy * dy);
+  sd = R - rho;
+  if (rho < 1e-12) return false;
+  n = normalised(Vec{dx / rho, dy / rho, -dRdz});
+  return true;
+}
+
 // Signed distance of p from the iolet plane (positive on the fluid side).
 inline double iolet_side(const Iolet& io, Vec p) { return dot(sub(p, io.pos), io.n); }
 
@@ -126,6 +152,7 @@ struct Geometry {
   std::vector<int32_t> iolet_id;
   std::vector<int8_t> site_type;
   std::vector<float> cuts;
+  std::vector<float> normals;  // per link site: unit wall normal, zero without wall links
   int64_t n_fluid = 0;
   bool with_cuts = false;
   // ensemble: member of each output block and per-member parameters
@@ -153,6 +180,7 @@ struct BlockOut {
   std::vector<int32_t> ioid;
   std::vector<int8_t> stype;
   std::vector<float> cuts;
+  std::vector<float> normals;
   int64_t nfluid = 0;
 };
 
@@ -281,6 +309,31 @@ struct Voxelizer {
             }
           }
           if (wm == 0 && im == 0) continue;
+          // wall normal: gradient of the shape the site lies deepest in; else the
+          // normalised sum of the wall-link vectors
+          Vec nrm{0, 0, 0};
+          if (wm) {
+            double best = -1e30;
+            bool got = false;
+            for (int sh : shp) {
+              double sdv;
+              Vec nv;
+              if (shape_normal(g.shapes[sh], p, sdv, nv) && sdv > best) {
+                best = sdv;
+                nrm = nv;
+                got = true;
+              }
+            }
+            if (!got) {
+              Vec acc{0, 0, 0};
+              for (int d = 1; d <= nl; ++d)
+                if ((wm >> (d - 1)) & 1u) acc = add(acc, Vec{(double)cx[d], (double)cy[d], (double)cz[d]});
+              if (dot(acc, acc) > 0) nrm = normalised(acc);
+            }
+          }
+          out.normals.push_back((float)nrm.x);
+          out.normals.push_back((float)nrm.y);
+          out.normals.push_back((float)nrm.z);
           out.local.push_back(l);
           out.wall.push_back(wm);
           out.iolet.push_back(im);
@@ -399,6 +452,7 @@ int voxelize(Geometry& g, int n_threads) {
       g.site_type.push_back(b.stype[s]);
     }
     if (g.with_cuts) g.cuts.insert(g.cuts.end(), b.cuts.begin(), b.cuts.end());
+    g.normals.insert(g.normals.end(), b.normals.begin(), b.normals.end());
     outs[t] = BlockOut();
   }
   return HLBG_OK;
@@ -678,6 +732,7 @@ int hlbg_synth_ensemble(uint64_t seed, int32_t n_members, int32_t q, int32_t n_t
       g->site_type.push_back(mg.site_type[r]);
     }
     g->cuts.insert(g->cuts.end(), mg.cuts.begin(), mg.cuts.end());
+    g->normals.insert(g->normals.end(), mg.normals.begin(), mg.normals.end());
     g->n_fluid += mg.n_fluid;
     g->member_sites.push_back(mg.n_fluid);
     Vec shift{8.0 * ox, 8.0 * oy, 0.0};
@@ -795,6 +850,7 @@ int hlbg_read_gmy(const char* path, int32_t q, void** handle) {
     int32_t ioid;
     int8_t type;
     float cut[26];
+    float normal[3];
   };
   std::vector<SiteRec> sites;
   size_t off = in.at;
@@ -849,10 +905,11 @@ int hlbg_read_gmy(const char* path, int32_t q, void** handle) {
           }
           const uint32_t has_normal = s.u32();
           if (has_normal > 1 || (has_normal == 1) != any_wall) return HLBG_ERR_INVAL;
+          r.normal[0] = r.normal[1] = r.normal[2] = 0.f;
           if (has_normal) {
-            s.f32();
-            s.f32();
-            s.f32();
+            r.normal[0] = s.f32();
+            r.normal[1] = s.f32();
+            r.normal[2] = s.f32();
           }
           if (!s.ok) return HLBG_ERR_INVAL;
           r.type = had_in ? HLBG_SITE_INLET : (had_out ? HLBG_SITE_OUTLET : HLBG_SITE_FLUID);
@@ -899,6 +956,7 @@ int hlbg_read_gmy(const char* path, int32_t q, void** handle) {
       g->iolet_id.push_back(r.ioid);
       g->site_type.push_back(r.type);
       for (int d = 0; d < q - 1; ++d) g->cuts.push_back(r.cut[d]);
+      for (int c = 0; c < 3; ++c) g->normals.push_back(r.normal[c]);
     }
   }
   *handle = g;
@@ -910,8 +968,9 @@ int hlbg_read_gmy(const char* path, int32_t q, void** handle) {
 int hlbg_write_gmy(const hlbg_geometry* g, const char* path) {
   // Inverse of hlbg_read_gmy with 8^3 blocks.  Lattice links keep their cut type,
   // iolet index and distance; Moore links outside the lattice are written as
-  // NONE.  Sites with a wall link get a wall normal (the normalised sum of their
-  // wall-link vectors), as the format requires one exactly for wall sites.
+  // NONE.  Sites with a wall link get a wall normal (the geometry's own, else the
+  // normalised sum of their wall-link vectors), as the format requires one exactly
+  // for wall sites.
 #if !HLBG_HAVE_ZLIB
   (void)g;
   (void)path;
@@ -1006,7 +1065,9 @@ int hlbg_write_gmy(const hlbg_geometry* g, const char* path) {
         put(raw, 0u);
       }
       put(raw, any_wall ? 1u : 0u);
-      if (any_wall) {
+      if (any_wall && g->wall_normal) {  // the geometry's own normal, as it is
+        for (int c = 0; c < 3; ++c) putf(raw, g->wall_normal[3 * r + c]);
+      } else if (any_wall) {
         double m = std::sqrt(nx * nx + ny * ny + nz * nz);
         if (m == 0) m = 1;
         putf(raw, (float)(nx / m));
@@ -1049,7 +1110,7 @@ int hlbg_synth_view(void* handle, hlbg_geometry* out, int64_t* n_fluid, int32_t*
   out->iolet_id = g->iolet_id.data();
   out->site_type = g->site_type.data();
   out->cut_distance = g->with_cuts ? g->cuts.data() : nullptr;
-  out->wall_normal = nullptr;
+  out->wall_normal = g->normals.size() == 3 * g->link_site.size() && !g->normals.empty() ? g->normals.data() : nullptr;
   if (n_fluid) *n_fluid = g->n_fluid;
   if (n_in) *n_in = (int32_t)g->inlets.size();
   if (n_outl) *n_outl = (int32_t)g->outlets.size();

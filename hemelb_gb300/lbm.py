@@ -55,6 +55,7 @@ class SyntheticGeometry:
         self.site_type = _np(v.site_type, n, np.int8)
         self.cut_distance = (_np(v.cut_distance, n * (v.q - 1), np.float32).reshape(n, v.q - 1)
                              if v.cut_distance else None)
+        self.wall_normal = _np(v.wall_normal, n * 3, np.float32).reshape(n, 3) if v.wall_normal else None
 
     def write_gmy(self, path: str):
         """Write this geometry as a HemeLB .gmy file (readable by GeometryReader)."""
@@ -323,6 +324,12 @@ class LBM:
         if rc not in (capi.HLBG_OK, capi.HLBG_ERR_UNSTABLE):
             check(rc, self._ctx)
         return st
+
+    def WallShearStress(self) -> np.ndarray:
+        """Wall shear stress magnitude per contiguous site (float max where no wall link)."""
+        out = np.empty(self.n_sites, dtype=np.float64)
+        check(self._lib.hlbg_wall_shear_stress(self._ctx, out.ctypes.data_as(_D)), self._ctx)
+        return out
 
     def Incompressibility(self) -> capi.Incomp:
         """IncompressibilityChecker's quantities of the last monitored step."""

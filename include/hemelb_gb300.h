@@ -96,7 +96,7 @@ typedef struct hlbg_geometry {
   const int32_t *iolet_id;      /* [n] iolet index (into the inlet or outlet list), -1 */
   const int8_t *site_type;      /* [n] HLBG_SITE_* */
   const float *cut_distance;    /* [n*(q-1)] link fraction to the surface, or NULL */
-  const float *wall_normal;     /* [n*3] or NULL (unused by the update) */
+  const float *wall_normal;     /* [n*3] or NULL: wall normal per link site (wall shear stress) */
 } hlbg_geometry;
 
 typedef struct hlbg_iolet {
@@ -252,6 +252,14 @@ int hlbg_run_to_steady(hlbg_ctx *ctx, double tol, double u_ref, int64_t max_step
  * Replaces hlbg_step + hlbg_reduce per step without re-reading both arrays
  * (Code/lb/StabilityTester.h:91-183). */
 int hlbg_step_monitored(hlbg_ctx *ctx, int32_t nsteps, hlbg_stats *out);
+/* Wall shear stress magnitude of every site of the current state, in contiguous
+ * site order (out[N]): Lattice::CalculateWallShearStressMagnitude on f_neq with the
+ * site's wall normal and LbmParameters' stress parameter (1 - 1/(2 tau)) / sqrt(2),
+ * as UpdateCachePostCollision fills wallShearStressMagnitudeCache
+ * (Code/lb/streamers/Common.h:35-52); DBL_MAX (NO_VALUE) where the site has no wall
+ * link.  Normals are the geometry's wall_normal, else the normalised sum of the
+ * site's wall-link vectors.  Computed in FP64 for every storage form. */
+int hlbg_wall_shear_stress(hlbg_ctx *ctx, double *out);
 /* IncompressibilityChecker for the state checked by the last monitored step
  * (hlbg_step_monitored or hlbg_run_to_steady): the densities and velocities are
  * those of the state each site collided, as the reference's property cache holds

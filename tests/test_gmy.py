@@ -40,6 +40,12 @@ def test_write_read_round_trip(tmp_path, maker):
     c1 = a1["cut"].reshape(o1.n, -1)[flagged.astype(bool)]
     c2 = a2["cut"].reshape(o2.n, -1)[flagged.astype(bool)]
     assert np.array_equal(c1, c2)
+    # the wall normals travel with the file (the format stores one per wall site)
+    assert np.array_equal(g.link_site, h.link_site)
+    wall = g.wall_mask != 0
+    assert g.wall_normal is not None and h.wall_normal is not None
+    assert np.allclose(np.linalg.norm(g.wall_normal[wall], axis=1), 1.0, atol=1e-6)
+    assert np.array_equal(g.wall_normal[wall], h.wall_normal[wall])
 
 
 @needs_ref

@@ -268,3 +268,73 @@ def test_every_launch_shape_gives_identical_distributions(precision):
             ref = f
         else:
             assert np.array_equal(f[0], ref[0]) and np.array_equal(f[1], ref[1]), v
+
+
+def _wss_reference(o, normals, tau, q=19):
+    """Lattice::CalculateWallShearStressMagnitude (Code/lb/lattices/Lattice.h:652-726)
+    restated step by step in FP64, on the oracle's state: moments and equilibrium
+    from the oracle's collision of each site, f_neq = f - f_eq."""
+    import ctypes as C
+    from oracle.oracle import Params, load
+    from tests.helpers import CX19, CY19, CZ19
+    lib = load()
+    p = Params()
+    p.q, p.kernel, p.tau = q, capi.KERNEL_LBGK, tau
+    V = list(zip(CX19, CY19, CZ19))
+    param = (1.0 - 1.0 / (2.0 * tau)) / np.sqrt(2.0)
+    f_all = o.fold()
+    a = o.arrays()
+    out = {}
+    for i in np.nonzero(a["wall_mask"] != 0)[0]:
+        f = np.ascontiguousarray(f_all[i])
+        rho, mom, vel, feq, fpost = np.zeros(1), np.zeros(3), np.zeros(3), np.zeros(q), np.zeros(q)
+        dp = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))
+        lib.hlbo_collide_site(C.byref(p), dp(f), dp(rho), dp(mom), dp(vel), dp(feq), dp(fpost))
+        fneq = [float(f[l] - feq[l]) for l in range(q)]
+        pi = [[0.0] * 3 for _ in range(3)]
+        for ii in range(3):
+            for jj in range(ii + 1):
+                acc = 0.0
+                for l in range(q):
+                    acc += fneq[l] * V[l][ii] * V[l][jj]
+                pi[ii][jj] = pi[jj][ii] = acc
+        nor = [float(x) for x in normals[i]]
+        temp = param * (-np.sqrt(2.0))
+        sq = nrm = 0.0
+        for ii in range(3):
+            sv = 0.0
+            for jj in range(3):
+                sv += pi[ii][jj] * nor[jj] * temp
+            sq += sv * sv
+            nrm += sv * nor[ii]
+        out[i] = np.sqrt(sq - nrm * nrm)
+    return out
+
+
+def test_wall_shear_stress_matches_reference_formula():
+    """Wall shear stress of every wall site after 300 steps (FP64) against the
+    reference's formula on the oracle's state, with the geometry's wall normals;
+    float max (NO_VALUE) elsewhere."""
+    c = small_bifurcation()
+    o = oracle_for(c)
+    o.step(300, THREADS)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(300)
+    w = s.WallShearStress()
+    g = c.geometry
+    a = o.arrays()
+    rec = {int(ls): k for k, ls in enumerate(g.link_site)}
+    normals = np.zeros((o.n, 3))
+    for i, slot in enumerate(a["slot"]):
+        k = rec.get(int(slot))
+        if k is not None:
+            normals[i] = g.wall_normal[k]
+    ref = _wss_reference(o, normals, c.params.tau)
+    wall = a["wall_mask"] != 0
+    assert len(ref) == wall.sum() > 100
+    got = np.array([w[i] for i in ref])
+    exp = np.array([ref[i] for i in ref])
+    assert np.all(np.abs(got - exp) <= 1e-12 * np.abs(exp).max())
+    assert np.all(w[~wall] == np.finfo(np.float64).max)
+    assert exp.max() > 0
