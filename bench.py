@@ -42,6 +42,12 @@ if WORLD > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
 import numpy as np  # noqa: E402
 
 B_ALG = {0: 304, 1: 152, 2: 76}  # algorithmic bytes per fluid-site update (2 * 19 * elem)
+# the update kernel each launch shape runs (hlbg_set_launch_variant)
+KERNEL_OF_VARIANT = {-1: "k_stream_collide<P, 128, 2>", 0: "k_stream_collide<P, 128, 10>",
+                     1: "k_stream_collide<P, 128, 8>", 2: "k_stream_collide<P, 256, 4>",
+                     3: "k_stream_collide<P, 512, 2>", 4: "k_stream_collide<P, 128, 10, persistent>",
+                     5: "k_stream_collide_listed<P, 128, 10>", 6: "k_stream_collide_listed<P, 128, 8>",
+                     7: "k_stream_collide_staged<128, 8, 4>"}
 DTYPE = {0: "f64", 1: "f32", 2: "f16-storage/f32"}
 METRIC = "fluid MLUPS (D3Q19 LB update)"
 
@@ -314,13 +320,17 @@ def main():
     per_launch = kms / args.steps
     peak, peak_kind = measured_peak()
     achieved = B_ALG[prec] * n / (per_launch / 1e3) / 1e9
-    tag = "k_stream_collide_%s_%s" % (args.precision, args.workload)
-    tps = profile_traffic(tag)
+    kname = KERNEL_OF_VARIANT.get(variant if prec != 0 else (5 if variant >= 5 else -1),
+                                  "k_stream_collide").replace("<P", "<%d" % prec)
+    base = kname.split("<")[0]
+    # DRAM bytes per site: a one-pass capture of this workload, else a small-case full capture
+    tps = profile_traffic("%s_%s_%s_dram" % (base, args.precision, args.workload)) \
+        or profile_traffic("%s_%s_%s" % (base, args.precision, args.workload))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": (tps * n if tps is not None else None),
                 "algorithmic_bytes_per_launch": B_ALG[prec] * n,
-                "kernel": "hlbg::k_stream_collide<%d>" % prec, "launch_ms": per_launch}
+                "kernel": "hlbg::" + kname, "launch_ms": per_launch}
     # ---- end to end through the C ABI: per step, H2D of that step's iolet values,
     # the update with the StabilityTester fused into it, and the D2H read-back of
     # its stats (stability, mass, max |du| for the convergence test), synchronous
