@@ -570,20 +570,21 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   ctx->n_ps = (int64_t)ctx->h_ps_slot.size();
   ctx->nb = nb;
   ctx->nslot = nslot;
-  // Pack every block that is not entirely fluid: its fluid sites take slots
-  // 0 .. nf-1 in site order and its solid sites the rest, so a partly fluid block
-  // moves whole 32-byte sectors instead of every z-row that touches fluid.
-  // Everything above was built with slot = site; map it now.
+  // Packed builds (HLBG_PACK) pack every block that is not entirely fluid: its
+  // fluid sites take slots 0 .. nf-1 in site order and its solid sites the rest.
+  // Everything above was built with slot = local site index; map it now (every
+  // block: the in-block order of slot_in_block, packed blocks their own).
   std::vector<uint16_t> site2slot((size_t)nslot), slot2site((size_t)nslot);
   std::vector<uint8_t> packed((size_t)nb, 0);
   parallel_for(nb, [&](int64_t b) {
     int nf = 0;
     for (int w = 0; w < 8; ++w) nf += __builtin_popcountll(mask[b * 8 + w]);
     packed[b] = HLBG_PACK && nf < 512;
-    if (!packed[b]) {  // slot == site
+    if (!packed[b]) {  // the fixed in-block order of slot_in_block
       for (int l = 0; l < 512; ++l) {
-        site2slot[b * 512 + l] = (uint16_t)l;
-        slot2site[b * 512 + l] = (uint16_t)l;
+        const int j = slot_of_local(l);
+        site2slot[b * 512 + l] = (uint16_t)j;
+        slot2site[b * 512 + j] = (uint16_t)l;
       }
       return;
     }
@@ -1208,6 +1209,225 @@ int hlbg_step_monitored(hlbg_ctx* ctx, int32_t nsteps, hlbg_stats* out) {
   out->unstable_sites = valid ? (int64_t)r[3] : 0;
   out->time_step = valid ? (int64_t)ctx->t1 - 1 : -1;
   return valid && r[3] > 0.0 ? HLBG_ERR_UNSTABLE : HLBG_OK;
+}
+
+}  // extern "C"
+
+// ---- XTR distribution checkpoints (doc/dev/file-formats/extraction.md, version 5) ----
+namespace {
+
+struct XdrOut {
+  std::vector<uint8_t> b;
+  void u32(uint32_t v) {
+    for (int k = 3; k >= 0; --k) b.push_back((uint8_t)(v >> (8 * k)));
+  }
+  void u64(uint64_t v) {
+    for (int k = 7; k >= 0; --k) b.push_back((uint8_t)(v >> (8 * k)));
+  }
+  void f64(double d) {
+    uint64_t v;
+    std::memcpy(&v, &d, 8);
+    u64(v);
+  }
+  void str(const std::string& t) {  // XDR string: length, bytes, zero padding to 4
+    u32((uint32_t)t.size());
+    b.insert(b.end(), t.begin(), t.end());
+    while (b.size() % 4) b.push_back(0);
+  }
+};
+
+struct XdrIn {
+  const uint8_t* p;
+  size_t n, at = 0;
+  bool ok = true;
+  uint64_t get(int bytes) {
+    if (at + bytes > n) {
+      ok = false;
+      return 0;
+    }
+    uint64_t v = 0;
+    for (int k = 0; k < bytes; ++k) v = (v << 8) | p[at++];
+    return v;
+  }
+  uint32_t u32() { return (uint32_t)get(4); }
+  uint64_t u64() { return get(8); }
+  double f64() {
+    const uint64_t v = get(8);
+    double d;
+    std::memcpy(&d, &v, 8);
+    return d;
+  }
+  std::string str() {
+    const uint32_t len = u32();
+    if (!ok || at + len > n) {
+      ok = false;
+      return std::string();
+    }
+    std::string t((const char*)p + at, len);
+    at += (len + 3) / 4 * 4;
+    return t;
+  }
+};
+
+constexpr uint32_t kHemeLbMagic = 0x686c6221u, kXtrMagic = 0x78747204u, kXtrVersion = 5u;
+constexpr uint32_t kOffMagic = 0x6f666604u, kOffVersion = 1u, kTypeDouble = 1u;
+const char* const kDistField = "distributions";
+
+// Main header (60 bytes) and the one field header of a distribution checkpoint
+// (LocalPropertyOutput::PrepareHeader, Code/extraction/LocalPropertyOutput.cc).
+std::vector<uint8_t> checkpoint_header(uint64_t nsites, double voxel, const double origin[3]) {
+  XdrOut field;
+  field.str(kDistField);
+  field.u32(19);           // values per site
+  field.u32(kTypeDouble);  // full precision
+  field.u32(0);            // no offsets
+  XdrOut h;
+  h.u32(kHemeLbMagic);
+  h.u32(kXtrMagic);
+  h.u32(kXtrVersion);
+  h.f64(voxel);
+  for (int c = 0; c < 3; ++c) h.f64(origin ? origin[c] : 0.0);
+  h.u64(nsites);
+  h.u32(1);
+  h.u32((uint32_t)field.b.size());
+  h.b.insert(h.b.end(), field.b.begin(), field.b.end());
+  return h.b;
+}
+
+std::string offset_path(const std::string& xtr) {  // io::formats::offset::ExtractionToOffset
+  const size_t dot = xtr.rfind('.');
+  return dot == std::string::npos ? std::string() : xtr.substr(0, dot) + ".off";
+}
+
+}  // namespace
+
+extern "C" {
+
+int hlbg_write_checkpoint(hlbg_ctx* ctx, const char* path, uint64_t timestep, double voxel_size,
+                          const double origin[3], int32_t append) {
+  // One timestep record: the step number, then per site in contiguous order its
+  // grid position and its 19 distributions of the current state (the reference's
+  // GetFOld), as LocalPropertyOutput::Write does for a "distributions" field.
+  if (!ctx || !path) return HLBG_ERR_INVAL;
+  const std::string opath = offset_path(path);
+  if (opath.empty()) return fail(ctx, HLBG_ERR_INVAL, "checkpoint path needs an extension");
+  const int64_t n = ctx->nsites;
+  std::vector<double> f((size_t)n * 19);
+  std::vector<int32_t> xyz((size_t)n * 3);
+  int rc = hlbg_get_f(ctx, f.data(), 0);
+  if (!rc) rc = hlbg_site_coords(ctx, xyz.data());
+  if (rc) return rc;
+  const std::vector<uint8_t> head = checkpoint_header((uint64_t)n, voxel_size, origin);
+  XdrOut rec;
+  rec.b.reserve(8 + (size_t)n * (12 + 19 * 8));
+  rec.u64(timestep);
+  for (int64_t i = 0; i < n; ++i) {
+    for (int c = 0; c < 3; ++c) rec.u32((uint32_t)xyz[3 * i + c]);
+    for (int d = 0; d < 19; ++d) rec.f64(f[(size_t)i * 19 + d]);
+  }
+  FILE* fp = append ? std::fopen(path, "rb") : nullptr;
+  if (fp) {  // append to a file of the same geometry
+    std::vector<uint8_t> old(head.size());
+    const bool same = std::fread(old.data(), 1, old.size(), fp) == old.size() &&
+                      std::memcmp(old.data() + 48, head.data() + 48, head.size() - 48) == 0;
+    std::fclose(fp);
+    if (!same) return fail(ctx, HLBG_ERR_INVAL, "checkpoint file holds another geometry");
+    fp = std::fopen(path, "ab");
+    if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot open checkpoint file");
+    const bool ok = std::fwrite(rec.b.data(), 1, rec.b.size(), fp) == rec.b.size();
+    std::fclose(fp);
+    return ok ? HLBG_OK : fail(ctx, HLBG_ERR_INVAL, "checkpoint write failed");
+  }
+  fp = std::fopen(path, "wb");
+  if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot create checkpoint file");
+  bool ok = std::fwrite(head.data(), 1, head.size(), fp) == head.size() &&
+            std::fwrite(rec.b.data(), 1, rec.b.size(), fp) == rec.b.size();
+  std::fclose(fp);
+  // offset file: one rank, its chunk of the first timestep (LocalPropertyOutput::WriteOffsetFile)
+  XdrOut off;
+  off.u32(kHemeLbMagic);
+  off.u32(kOffMagic);
+  off.u32(kOffVersion);
+  off.u32(1);  // int32 rank count
+  off.u64(head.size());
+  off.u64(head.size() + rec.b.size());
+  FILE* fo = std::fopen(opath.c_str(), "wb");
+  ok = ok && fo && std::fwrite(off.b.data(), 1, off.b.size(), fo) == off.b.size();
+  if (fo) std::fclose(fo);
+  return ok ? HLBG_OK : fail(ctx, HLBG_ERR_INVAL, "checkpoint write failed");
+}
+
+int hlbg_read_checkpoint(hlbg_ctx* ctx, const char* path, int64_t timestep, uint64_t* found) {
+  // LocalDistributionInput::LoadDistribution (Code/extraction/LocalDistributionInput.cc:
+  // 56-251): the header checks, the record of the requested timestep (the last one
+  // if timestep < 0), each site's grid position against this geometry's contiguous
+  // order, and the distributions into both time levels.
+  if (!ctx || !path) return HLBG_ERR_INVAL;
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot open checkpoint file");
+  std::vector<uint8_t> buf;
+  {
+    std::fseek(fp, 0, SEEK_END);
+    const long sz = std::ftell(fp);
+    std::fseek(fp, 0, SEEK_SET);
+    buf.resize(sz > 0 ? (size_t)sz : 0);
+    const size_t got = std::fread(buf.data(), 1, buf.size(), fp);
+    std::fclose(fp);
+    if (got != buf.size()) return fail(ctx, HLBG_ERR_INVAL, "checkpoint read failed");
+  }
+  XdrIn in{buf.data(), buf.size()};
+  if (in.u32() != kHemeLbMagic || in.u32() != kXtrMagic) return fail(ctx, HLBG_ERR_INVAL, "not an extraction file");
+  if (in.u32() != kXtrVersion) return fail(ctx, HLBG_ERR_INVAL, "extraction version is not 5");
+  for (int k = 0; k < 4; ++k) in.f64();  // voxel size, origin
+  const uint64_t nsites = in.u64();
+  const uint32_t nfields = in.u32(), fhl = in.u32();
+  const size_t field_start = in.at;
+  const std::string name = in.str();
+  const uint32_t nelem = in.u32(), type = in.u32(), noff = in.u32();
+  if (!in.ok || nfields != 1 || name != kDistField || nelem != 19 || type != kTypeDouble || noff != 0 ||
+      in.at - field_start != fhl)
+    return fail(ctx, HLBG_ERR_INVAL, "not a D3Q19 distribution checkpoint");
+  if ((int64_t)nsites != ctx->nsites) return fail(ctx, HLBG_ERR_INVAL, "checkpoint site count differs");
+  const size_t head = in.at, rec = 8 + (size_t)nsites * (12 + 19 * 8);
+  if ((buf.size() - head) % rec || buf.size() == head)
+    return fail(ctx, HLBG_ERR_INVAL, "checkpoint length is not a whole number of timesteps");
+  const size_t nt = (buf.size() - head) / rec;
+  auto ts_at = [&](size_t k) {
+    XdrIn t{buf.data() + head + k * rec, 8};
+    return t.u64();
+  };
+  size_t k = nt - 1;
+  if (timestep >= 0) {  // the timesteps are increasing: binary search
+    size_t lo = 0, len = nt;
+    while (len) {
+      const size_t half = len / 2, m = lo + half;
+      if (ts_at(m) < (uint64_t)timestep) {
+        lo = m + 1;
+        len -= half + 1;
+      } else {
+        len = half;
+      }
+    }
+    if (lo >= nt || ts_at(lo) != (uint64_t)timestep)
+      return fail(ctx, HLBG_ERR_INVAL, "timestep not found in checkpoint file");
+    k = lo;
+  }
+  std::vector<int32_t> xyz((size_t)nsites * 3);
+  int rc = hlbg_site_coords(ctx, xyz.data());
+  if (rc) return rc;
+  XdrIn d{buf.data() + head + k * rec, rec};
+  const uint64_t ts = d.u64();
+  std::vector<double> f((size_t)nsites * 19);
+  for (uint64_t i = 0; i < nsites; ++i) {
+    for (int c = 0; c < 3; ++c)
+      if ((int32_t)d.u32() != xyz[3 * i + c])
+        return fail(ctx, HLBG_ERR_INVAL, "site " + std::to_string(i) + " of the checkpoint is not this geometry's");
+    for (int q = 0; q < 19; ++q) f[i * 19 + q] = d.f64();
+  }
+  if (!d.ok) return fail(ctx, HLBG_ERR_INVAL, "truncated checkpoint");
+  if ((rc = hlbg_put_f(ctx, f.data(), 0)) || (rc = hlbg_put_f(ctx, f.data(), 1))) return rc;
+  if (found) *found = ts;
+  return HLBG_OK;
 }
 
 int hlbg_wall_shear_stress(hlbg_ctx* ctx, double* out) {

@@ -79,7 +79,8 @@ struct GlobalBase {
   __device__ __forceinline__ int32_t operator()(int k) const { return __ldg(tab + k); }
 };
 
-// Slot of local site tl in the block of table entry e (e >= 0).
+// Slot of the slot-in-block tl (slot_in_block of the target's local coordinates;
+// in packed builds its local site index) in the block of table entry e (e >= 0).
 __device__ __forceinline__ int64_t target_slot(const StepArgs& a, int32_t e, int tl) {
 #if HLBG_PACK
   const int64_t nb = e & ~kPackedBit;
@@ -89,7 +90,7 @@ __device__ __forceinline__ int64_t target_slot(const StepArgs& a, int32_t e, int
   return ((int64_t)e << 9) + tl;
 #endif
 }
-// Element offset of direction D of local site tl in the block of entry e (e >= 0).
+// Element offset of direction D of slot-in-block tl in the block of entry e (e >= 0).
 __device__ __forceinline__ int64_t target_off(const StepArgs& a, int32_t e, int D, int tl) {
 #if HLBG_PACK
   const int32_t nb = e & ~kPackedBit;
@@ -104,7 +105,7 @@ __device__ __forceinline__ int site_of_slot(const StepArgs& a, int64_t s, bool p
 #if HLBG_PACK
   return packed ? (int)__ldg(a.slot2site + s) : (int)(s & (kSites - 1));
 #else
-  return (int)(s & (kSites - 1));
+  return local_of_slot((int)(s & (kSites - 1)));
 #endif
 }
 
@@ -153,7 +154,7 @@ struct BoundaryAll {
       constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
       const int xx = x + cx, yy = y + cy, zz = z + cz;
       const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
-      const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+      const int tl = slot_in_block(xx & 7, yy & 7, zz & 7);
       const int32_t e = base(k);
       if (e >= 0) {
         const int64_t ns = target_slot(a, e, tl);
@@ -183,7 +184,7 @@ struct PushAll {
     constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
     const int xx = x + cx, yy = y + cy, zz = z + cz;
     const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
-    const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+    const int tl = slot_in_block(xx & 7, yy & 7, zz & 7);
     Store<P>::store(fn, target_off(a, base(k), D, tl), fpost[D], a);
     PushAll<P, D + 1>::run(fn, a, base, x, y, z, fpost);
   }
@@ -204,7 +205,7 @@ struct PushBulk {
     constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
     const int xx = x + cx, yy = y + cy, zz = z + cz;
     const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
-    const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+    const int tl = slot_in_block(xx & 7, yy & 7, zz & 7);
     const int32_t e = base(k);  // every lane shuffles
     if (store) Store<P>::store(fn, target_off(a, e, D, tl), fpost[D], a);
     push_fence();
@@ -235,7 +236,7 @@ struct PushMixed {
     constexpr int inv = Lat::inv(D);
     const int xx = x + cx, yy = y + cy, zz = z + cz;
     const int k = 13 + 9 * (xx >> 3) + 3 * (yy >> 3) + (zz >> 3);
-    const int tl = ((xx & 7) << 6) | ((yy & 7) << 3) | (zz & 7);
+    const int tl = slot_in_block(xx & 7, yy & 7, zz & 7);
     const int32_t e = base(k);  // every lane shuffles
     const unsigned lc = (unsigned)((links >> (3 * D)) & 7u);
     int64_t off = 0;

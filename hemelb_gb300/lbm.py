@@ -325,6 +325,26 @@ class LBM:
             check(rc, self._ctx)
         return st
 
+    def WriteCheckpoint(self, path: str, timestep: int, voxel_size: float = 1.0, origin=(0.0, 0.0, 0.0),
+                        append: bool = False):
+        """XTR (version 5) distribution checkpoint of the current state."""
+        o = (C.c_double * 3)(*origin)
+        check(self._lib.hlbg_write_checkpoint(self._ctx, path.encode(), timestep, voxel_size, o, int(append)),
+              self._ctx)
+
+    def ReadCheckpoint(self, path: str, timestep: int = -1) -> int:
+        """Load a distribution checkpoint (its last record when timestep < 0) into both
+        time levels; returns the record's timestep.  The step counter is left alone,
+        as LocalDistributionInput leaves it to the initial condition's SetTime:
+        SetTimeStep sets the step of the next update."""
+        t = C.c_uint64()
+        check(self._lib.hlbg_read_checkpoint(self._ctx, path.encode(), timestep, C.byref(t)), self._ctx)
+        return int(t.value)
+
+    def SetTimeStep(self, t1: int):
+        """1-indexed time step of the next update (SimulationState::timeStep)."""
+        check(self._lib.hlbg_set_time_step(self._ctx, t1), self._ctx)
+
     def WallShearStress(self) -> np.ndarray:
         """Wall shear stress magnitude per contiguous site (float max where no wall link)."""
         out = np.empty(self.n_sites, dtype=np.float64)
@@ -336,6 +356,15 @@ class LBM:
         out = capi.Incomp()
         check(self._lib.hlbg_incompressibility(self._ctx, C.byref(out)), self._ctx)
         return out
+
+    def IsDensityDiffWithinRange(self, allowed: float = 0.05) -> bool:
+        """IncompressibilityChecker::IsDensityDiffWithinRange with its default 5 %
+        (Code/lb/IncompressibilityChecker.hpp:247-250)."""
+        return self.Incompressibility().max_relative_density_difference < allowed
+
+    def MaxMachNumber(self) -> float:
+        """Largest velocity magnitude over the lattice sound speed 1/sqrt(3)."""
+        return self.Incompressibility().max_velocity * 3.0 ** 0.5
 
     def AverageTimeLevels(self):
         """Current distributions <- mean of the two time levels (right after a step)."""

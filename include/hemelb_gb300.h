@@ -252,6 +252,19 @@ int hlbg_run_to_steady(hlbg_ctx *ctx, double tol, double u_ref, int64_t max_step
  * Replaces hlbg_step + hlbg_reduce per step without re-reading both arrays
  * (Code/lb/StabilityTester.h:91-183). */
 int hlbg_step_monitored(hlbg_ctx *ctx, int32_t nsteps, hlbg_stats *out);
+/* XTR distribution checkpoints (doc/dev/file-formats/extraction.md, version 5): one
+ * field "distributions" of 19 doubles per site, sites in contiguous order with their
+ * grid positions, one record per timestep, and the ".off" offset file of a single
+ * rank, as LocalPropertyOutput writes them (Code/extraction/LocalPropertyOutput.cc)
+ * and LocalDistributionInput reads them (LocalDistributionInput.cc:56-251).
+ * hlbg_write_checkpoint writes the current state (the reference's fOld) at
+ * `timestep`; with append != 0 it adds a record to an existing file of the same
+ * geometry.  hlbg_read_checkpoint loads the record of `timestep` (the last one when
+ * timestep < 0) into both time levels after checking every site's position, and
+ * reports the timestep it found. */
+int hlbg_write_checkpoint(hlbg_ctx *ctx, const char *path, uint64_t timestep, double voxel_size,
+                          const double origin[3], int32_t append);
+int hlbg_read_checkpoint(hlbg_ctx *ctx, const char *path, int64_t timestep, uint64_t *found);
 /* Wall shear stress magnitude of every site of the current state, in contiguous
  * site order (out[N]): Lattice::CalculateWallShearStressMagnitude on f_neq with the
  * site's wall normal and LbmParameters' stress parameter (1 - 1/(2 tau)) / sqrt(2),

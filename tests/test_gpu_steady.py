@@ -130,5 +130,8 @@ def test_incompressibility_checker_of_the_monitored_state(prec):
         assert abs(inc.min_density - rho.min()) <= tol and abs(inc.max_density - rho.max()) <= tol
         assert abs(inc.max_velocity - umag.max()) <= tol * max(1.0, umag.max()) + (0 if prec == capi.FP64 else 1e-7)
         assert abs(inc.max_relative_density_difference - (inc.max_density - inc.min_density)) <= 1e-15
+    assert a.IsDensityDiffWithinRange() == (inc.max_relative_density_difference < 0.05)
+    assert not a.IsDensityDiffWithinRange(allowed=0.0)
+    assert abs(a.MaxMachNumber() - inc.max_velocity * np.sqrt(3.0)) <= 1e-15
     a.close()
     b.close()
