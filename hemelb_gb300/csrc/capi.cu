@@ -627,7 +627,7 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     };
     for (int64_t b = 0; b < nb; ++b) {
       for (int j = 0; j < 512; ++j)
-        if (code[b * 512 + j]) tmp.push_back((uint16_t)j);
+        if (code[b * 512 + j]) tmp.push_back((uint16_t)(j | (code[b * 512 + j] >= 2 ? kListBoundary : 0u)));
       flush(b, false);
       for (int sec = 0; sec < 64; ++sec) {
         bool any = false;

@@ -82,6 +82,8 @@ struct IoletDev {
 
 // Flag of a block_nbr entry whose block has its fluid sites packed (slot != site).
 constexpr int32_t kPackedBit = 1 << 30;
+// Flag of a fluid-list entry whose site has a boundary record (site_code >= 2).
+constexpr unsigned kListBoundary = 1u << 14;
 // HLBG_PACK=1 builds the packed layout (fluid sites of partly fluid blocks in the
 // first slots).  It moves 5-12% fewer bytes but the slot lookups of the pushes cost
 // more than that saves (measured on the vascular forest), so the default is off.
@@ -89,13 +91,15 @@ constexpr int32_t kPackedBit = 1 << 30;
 #define HLBG_PACK 0
 #endif
 
-// Order of the 512 slots of a block.  HLBG_BLOCK_ORDER=1 (default): the bits of
-// the site's local (x, y, z) interleaved, z fastest, so the eight slots of one
-// 32-byte sector of FP32 values hold a 2x2x2 cube of sites (FP64: 1x2x2; FP16:
-// 2x2x4).  0: z-rows, slot = (x*8 + y)*8 + z, a sector being a 1x1x8 row.  A
-// vessel wall cuts fewer cubes than rows: on the vascular forest the sectors
-// touched per fluid site drop from 1.22 to 1.10 (FP32), and every sector touched
-// is read and written whole.
+// Order of the 512 slots of a block.  HLBG_BLOCK_ORDER=0 (default): z-rows,
+// slot = (x*8 + y)*8 + z, so a 32-byte sector of FP32 values is a 1x1x8 row.  1:
+// the bits of the local (x, y, z) interleaved, z fastest, a sector being a 2x2x2
+// cube (FP64: 1x2x2; FP16: 2x2x4).  Cubes cut by vessel walls are fewer (sectors
+// touched per fluid site 1.06 instead of 1.14 on the vascular forest), but a cube
+// on an x or y face of a block is then written by two blocks that the z-column
+// launch order runs far apart, so its halves leave L2 separately: measured, the
+// DRAM bytes did not drop and the update was 9% slower.  Rows only split across z
+// faces, between blocks that run back to back.
 #ifndef HLBG_BLOCK_ORDER
 #define HLBG_BLOCK_ORDER 0
 #endif
@@ -140,8 +144,9 @@ struct StepArgs {
   int64_t mon_nparts;
   const int32_t* mon_state;
   // Fluid-list launch: warp w works on block warp_block[w] & 0x7fffffff, lane k on
-  // its slot lane_slot[32 w + k] (0xffff: idle); a negative warp_block marks a warp
-  // that only writes zeros into the solid slots sharing a 32-byte sector with fluid.
+  // its slot lane_slot[32 w + k] & 511 (0xffff: idle; kListBoundary set for a site
+  // with a boundary record); a negative warp_block marks a warp that only writes
+  // zeros into the solid slots sharing a 32-byte sector with fluid.
   const int32_t* warp_block;
   const uint16_t* lane_slot;
   int64_t n_warps;

@@ -390,15 +390,31 @@ __device__ __forceinline__ MonAcc mon_block_f(MonAccF v) {
 // CalculateDensityAndMomentum), against the one recorded when this site was last
 // updated; f > 0 over all directions; the density for the mass.  The new velocity
 // is recorded for the next step.
+// The velocity recorded at a site's last update, loaded before the site's
+// distributions are used so that its latency overlaps theirs.
+template <int P>
+struct MonOld {
+  using U = typename std::conditional<P == 0, double, float>::type;
+  U x = 0, y = 0, z = 0;
+  __device__ __forceinline__ void load(const StepArgs& a, int64_t s, bool want) {
+    if (!want) return;
+    const int64_t ui = (s >> 9) * (3 * kSites) + (s & (kSites - 1));
+    const U* u = static_cast<const U*>(a.mon_u);
+    x = u[ui];
+    y = u[ui + kSites];
+    z = u[ui + 2 * kSites];
+  }
+};
+
 template <int P>
 __device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const double* f, double m0, double mx,
-                                         double my, double mz, MonAcc& acc, bool check) {
+                                         double my, double mz, MonAcc& acc, bool check, const MonOld<P>& uo) {
   // FP64 form: the reference's arithmetic (m / rho, |du| by inner product)
   const int64_t ui = (s >> 9) * (3 * kSites) + (s & (kSites - 1));
   double* u = static_cast<double*>(a.mon_u);
   const double ux = mx / m0, uy = my / m0, uz = mz / m0;
   if (check) {
-    const double dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
+    const double dx = ux - uo.x, dy = uy - uo.y, dz = uz - uo.z;
     const double du = sqrt(dot3d(dx, dy, dz, dx, dy, dz));
     if (!(du <= acc.maxdu)) acc.maxdu = du;
     acc.mass += m0;
@@ -423,14 +439,14 @@ __device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const dou
 
 template <int P>
 __device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const float* f, float m0, float mx,
-                                         float my, float mz, MonAccF& acc, bool check) {
+                                         float my, float mz, MonAccF& acc, bool check, const MonOld<P>& uo) {
   // deviation forms: m0 = rho - 1
   const int64_t ui = (s >> 9) * (3 * kSites) + (s & (kSites - 1));
   float* u = static_cast<float*>(a.mon_u);
   const float ir = 1.f / (1.f + m0);
   const float ux = mx * ir, uy = my * ir, uz = mz * ir;
   if (check) {
-    const float dx = ux - u[ui], dy = uy - u[ui + kSites], dz = uz - u[ui + 2 * kSites];
+    const float dx = ux - uo.x, dy = uy - uo.y, dz = uz - uo.z;
     const float du = sqrtf(dx * dx + dy * dy + dz * dz);
     if (!(du <= acc.maxdu)) acc.maxdu = du;
     acc.dm += m0;
@@ -519,6 +535,8 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
   const int l = site_of_slot(a, s, packed);
   const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + j;
   S* fn = static_cast<S*>(a.f_new);
+  MonOld<P> uo;
+  if constexpr (MON) uo.load(a, s, check && code != 0);
   T f[Q], fpost[Q];
   if (code != 0) {
 #pragma unroll
@@ -530,7 +548,7 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
   T m0, mx, my, mz;
   collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
   if constexpr (MON) {
-    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check);
+    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check, uo);
   }
   const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
   const bool bnd = code >= 2;
@@ -564,7 +582,7 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   const int64_t b = e & 0x7fffffff;
   const unsigned js = __ldg(a.lane_slot + w * 32 + lane);
   const bool on = js != 0xffffu;
-  const int j = on ? (int)js : 0;
+  const int j = on ? (int)(js & (kSites - 1)) : 0;
   const int64_t s = b * kSites + j;
   S* fn = static_cast<S*>(a.f_new);
   if (e < 0) {  // zero-fill warp: complete the sectors its slots share with fluid
@@ -576,12 +594,16 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   }
   const int32_t* tab = a.block_nbr + b * 27;
   const int32_t tabreg = lane < 27 ? __ldg(tab + lane) : 0;
-  const uint32_t code = on ? (a.block_bulk[b] ? 1u : a.site_code[s]) : 0u;
+  // every listed lane is a fluid site: its loads need not wait for its code, and
+  // only the boundary sites (flagged in the list) read one
+  const uint32_t code = on ? ((js & kListBoundary) ? a.site_code[s] : 1u) : 0u;
   const bool packed = (__shfl_sync(0xffffffffu, tabreg, 13) & kPackedBit) != 0;
   const int l = on ? site_of_slot(a, s, packed) : 0;
   const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + j;
+  MonOld<P> uo;
+  if constexpr (MON) uo.load(a, s, check && on);
   T f[Q], fpost[Q];
-  if (code != 0) {
+  if (on) {
     if constexpr (STAGED) {
 #pragma unroll
       for (int i = 0; i < Q; ++i) f[i] = staged[i * kStageStride];
@@ -596,7 +618,7 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   T m0, mx, my, mz;
   collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
   if constexpr (MON) {
-    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check);
+    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check, uo);
   }
   const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
   const bool bnd = code >= 2;
@@ -632,7 +654,7 @@ __device__ __forceinline__ void stage_unit(const StepArgs& a, int64_t u, float* 
   if (e < 0) return;  // a zero-fill warp reads nothing
   const unsigned js = __ldg(a.lane_slot + u * 32 + (threadIdx.x & 31));
   if (js == 0xffffu) return;
-  const float* src = static_cast<const float*>(a.f_old) + (int64_t)e * (Q * kSites) + js;
+  const float* src = static_cast<const float*>(a.f_old) + (int64_t)e * (Q * kSites) + (js & (kSites - 1));
 #pragma unroll
   for (int d = 0; d < Q; ++d) cp_async4(dst + d * kStageStride, src + d * kSites);
 }
