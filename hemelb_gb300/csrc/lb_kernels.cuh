@@ -1242,7 +1242,7 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     if (a.mon_u && (variant == 0 || variant == 4)) variant = 1;                                  \
     if (a.mon_u && variant == 5) variant = 6;                                                   \
     if (variant == 5) {                                                                         \
-      launch_listed<P, 128, (P == 0 ? 2 : 10), false>(a, bxyz, st);                             \
+      launch_listed<P, 128, (P == 0 ? 2 : 9), false>(a, bxyz, st);                              \
       return;                                                                                   \
     }                                                                                           \
     if (variant == 7) {                                                                         \
