@@ -350,46 +350,31 @@ __device__ __forceinline__ void mon_combine_f(MonAccF& a, const MonAccF& b) {
   a.count += b.count;
   a.bad += b.bad;
 }
-// CTA-wide: FP32 within each warp, FP64 across the warps' results; valid in thread 0.
-__device__ __forceinline__ MonAcc mon_block_f(MonAccF v) {
-  for (int off = 16; off > 0; off >>= 1) {
-    MonAccF o;
-    o.dm = __shfl_down_sync(0xffffffffu, v.dm, off);
-    o.maxdu = __shfl_down_sync(0xffffffffu, v.maxdu, off);
-    o.minf = __shfl_down_sync(0xffffffffu, v.minf, off);
-    o.dmin = __shfl_down_sync(0xffffffffu, v.dmin, off);
-    o.dmax = __shfl_down_sync(0xffffffffu, v.dmax, off);
-    o.umax = __shfl_down_sync(0xffffffffu, v.umax, off);
-    o.count = __shfl_down_sync(0xffffffffu, v.count, off);
-    o.bad = __shfl_down_sync(0xffffffffu, v.bad, off);
-    mon_combine_f(v, o);
-  }
-  MonAcc d = mon_neutral();
-  if (v.count) {
-    d.mass = (double)v.count + (double)v.dm;
-    d.maxdu = (double)v.maxdu;
-    d.minf = (double)v.minf;
-    d.bad = v.bad;
-    d.rmin = 1.0 + (double)v.dmin;
-    d.rmax = 1.0 + (double)v.dmax;
-    d.umax = (double)v.umax;
-  }
-  __shared__ MonAcc sh[32];
+// CTA-wide, in FP32 and integers throughout (a fixed order); valid in thread 0.
+__device__ __forceinline__ MonAccF mon_shfl_f(const MonAccF& v, int off) {
+  MonAccF o;
+  o.dm = __shfl_down_sync(0xffffffffu, v.dm, off);
+  o.maxdu = __shfl_down_sync(0xffffffffu, v.maxdu, off);
+  o.minf = __shfl_down_sync(0xffffffffu, v.minf, off);
+  o.dmin = __shfl_down_sync(0xffffffffu, v.dmin, off);
+  o.dmax = __shfl_down_sync(0xffffffffu, v.dmax, off);
+  o.umax = __shfl_down_sync(0xffffffffu, v.umax, off);
+  o.count = __shfl_down_sync(0xffffffffu, v.count, off);
+  o.bad = __shfl_down_sync(0xffffffffu, v.bad, off);
+  return o;
+}
+__device__ __forceinline__ MonAccF mon_block_f(MonAccF v) {
+  __shared__ MonAccF sh[32];
+  for (int off = 16; off > 0; off >>= 1) mon_combine_f(v, mon_shfl_f(v, off));
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) sh[w] = d;
+  if (lane == 0) sh[w] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) mon_combine(d, sh[k]);
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) mon_combine_f(v, sh[k]);
   }
-  return d;
+  return v;
 }
 
-// Fused StabilityTester for one fluid site of a monitored step
-// (Code/lb/StabilityTester.h:91-183): the velocity of the state being collided,
-// m / rho with the moments of the collision (the reference's
-// CalculateDensityAndMomentum), against the one recorded when this site was last
-// updated; f > 0 over all directions; the density for the mass.  The new velocity
-// is recorded for the next step.
 // The velocity recorded at a site's last update, loaded before the site's
 // distributions are used so that its latency overlaps theirs.
 template <int P>
@@ -406,6 +391,12 @@ struct MonOld {
   }
 };
 
+// Fused StabilityTester for one fluid site of a monitored step
+// (Code/lb/StabilityTester.h:91-183): the velocity of the state being collided,
+// m / rho with the moments of the collision (the reference's
+// CalculateDensityAndMomentum), against the one recorded when this site was last
+// updated; f > 0 over all directions; the density for the mass.  The new velocity
+// is recorded for the next step.
 template <int P>
 __device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const double* f, double m0, double mx,
                                          double my, double mz, MonAcc& acc, bool check, const MonOld<P>& uo) {
@@ -477,9 +468,38 @@ template <int P>
 __device__ __forceinline__ MonAccT<P> mon_neutral_t() {
   if constexpr (P == 0) return mon_neutral(); else return mon_neutral_f();
 }
+// One CTA's monitor partial: FP64 form as 7 doubles [mass | max |du| | min f |
+// unstable | min rho | max rho | max |u|], stride mon_nparts; FP32 forms as 8
+// 32-bit words [sum (rho-1) | max |du| | min f | min (rho-1) | max (rho-1) | max |u|
+// | count | unstable] in the same buffer, converted to FP64 by the second stage.
 template <int P>
-__device__ __forceinline__ MonAcc mon_block_t(const MonAccT<P>& v) {
-  if constexpr (P == 0) return mon_block(v); else return mon_block_f(v);
+__device__ __forceinline__ void mon_write_partial(const StepArgs& a, const MonAccT<P>& acc) {
+  const int64_t n = a.mon_nparts;
+  if constexpr (P == 0) {
+    const MonAcc r = mon_block(acc);
+    if (threadIdx.x == 0) {
+      a.mon_part[blockIdx.x] = r.mass;
+      a.mon_part[n + blockIdx.x] = r.maxdu;
+      a.mon_part[2 * n + blockIdx.x] = r.minf;
+      a.mon_part[3 * n + blockIdx.x] = (double)r.bad;
+      a.mon_part[4 * n + blockIdx.x] = r.rmin;
+      a.mon_part[5 * n + blockIdx.x] = r.rmax;
+      a.mon_part[6 * n + blockIdx.x] = r.umax;
+    }
+  } else {
+    const MonAccF r = mon_block_f(acc);
+    if (threadIdx.x == 0) {
+      float* p = reinterpret_cast<float*>(a.mon_part);
+      p[blockIdx.x] = r.dm;
+      p[n + blockIdx.x] = r.maxdu;
+      p[2 * n + blockIdx.x] = r.minf;
+      p[3 * n + blockIdx.x] = r.dmin;
+      p[4 * n + blockIdx.x] = r.dmax;
+      p[5 * n + blockIdx.x] = r.umax;
+      p[6 * n + blockIdx.x] = __uint_as_float(r.count);
+      p[7 * n + blockIdx.x] = __uint_as_float(r.bad);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -693,19 +713,7 @@ __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArg
   bool check = false;
   if constexpr (MON) check = *a.mon_state != 0;
   collide_listed_warp<P, MON>(a, ((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5, block_xyz, acc, check);
-  if constexpr (MON) {
-    const MonAcc r = mon_block_t<P>(acc);
-    if (threadIdx.x == 0) {
-      const int64_t n = a.mon_nparts;
-      a.mon_part[blockIdx.x] = r.mass;
-      a.mon_part[n + blockIdx.x] = r.maxdu;
-      a.mon_part[2 * n + blockIdx.x] = r.minf;
-      a.mon_part[3 * n + blockIdx.x] = (double)r.bad;
-      a.mon_part[4 * n + blockIdx.x] = r.rmin;
-      a.mon_part[5 * n + blockIdx.x] = r.rmax;
-      a.mon_part[6 * n + blockIdx.x] = r.umax;
-    }
-  }
+  if constexpr (MON) mon_write_partial<P>(a, acc);
 }
 
 template <int P, int THREADS, int MINB, bool MON>
@@ -730,31 +738,30 @@ __global__ void __launch_bounds__(THREADS, MINB)
     for (int64_t c = blockIdx.x; c < nchunk; c += gridDim.x)
       collide_slot<P, MON>(a, c * THREADS + threadIdx.x, block_xyz, acc, check);
   }
-  if constexpr (MON) {
-    const MonAcc r = mon_block_t<P>(acc);
-    if (threadIdx.x == 0) {
-      const int64_t n = a.mon_nparts;
-      a.mon_part[blockIdx.x] = r.mass;
-      a.mon_part[n + blockIdx.x] = r.maxdu;
-      a.mon_part[2 * n + blockIdx.x] = r.minf;
-      a.mon_part[3 * n + blockIdx.x] = (double)r.bad;
-      a.mon_part[4 * n + blockIdx.x] = r.rmin;
-      a.mon_part[5 * n + blockIdx.x] = r.rmax;
-      a.mon_part[6 * n + blockIdx.x] = r.umax;
-    }
-  }
+  if constexpr (MON) mon_write_partial<P>(a, acc);
 }
 
 // Second stage of the fused StabilityTester's reduction: CTA c folds partials
 // [c * per, (c + 1) * per) in a fixed order into out[c] (same layout, stride n_out).
+// fp32 != 0: the partials are the FP32 forms' 32-bit words (mon_write_partial).
 static __global__ void __launch_bounds__(256) k_mon_stage2(const double* __restrict__ in, int64_t n_in,
                                                            int64_t per, double* __restrict__ out,
-                                                           int64_t n_out) {
+                                                           int64_t n_out, int fp32) {
   MonAcc acc = mon_neutral();
   const int64_t lo = (int64_t)blockIdx.x * per, hi = lo + per < n_in ? lo + per : n_in;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-    mon_combine(acc, MonAcc{in[i], in[n_in + i], in[2 * n_in + i], (unsigned long long)in[3 * n_in + i],
-                            in[4 * n_in + i], in[5 * n_in + i], in[6 * n_in + i]});
+  const float* inf = reinterpret_cast<const float*>(in);
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    if (fp32) {
+      const unsigned count = __float_as_uint(inf[6 * n_in + i]);
+      if (count == 0) continue;  // a CTA of idle lanes only
+      mon_combine(acc, MonAcc{(double)count + (double)inf[i], (double)inf[n_in + i], (double)inf[2 * n_in + i],
+                              (unsigned long long)__float_as_uint(inf[7 * n_in + i]), 1.0 + (double)inf[3 * n_in + i],
+                              1.0 + (double)inf[4 * n_in + i], (double)inf[5 * n_in + i]});
+    } else {
+      mon_combine(acc, MonAcc{in[i], in[n_in + i], in[2 * n_in + i], (unsigned long long)in[3 * n_in + i],
+                              in[4 * n_in + i], in[5 * n_in + i], in[6 * n_in + i]});
+    }
+  }
   __syncthreads();
   acc = mon_block(acc);
   if (threadIdx.x == 0) {
@@ -1290,7 +1297,7 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
                              int32_t* mon_state, double* result, const SteadyArgs& sa,          \
                              int steady, cudaStream_t st) {                                      \
     const int64_t per = (nparts + n2 - 1) / n2;                                                 \
-    k_mon_stage2<<<(unsigned)n2, 256, 0, st>>>(part, nparts, per, part2, n2);                   \
+    k_mon_stage2<<<(unsigned)n2, 256, 0, st>>>(part, nparts, per, part2, n2, P != 0);           \
     k_mon_final<<<1, 256, 0, st>>>(part2, n2, mon_state, result, sa, steady);                   \
   }                                                                                             \
   void launch_iolet_links_##P(const StepArgs& a, const int32_t* rec, const int32_t* rec_slot,    \
