@@ -542,6 +542,7 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   off[0] = 0;
   for (int t = 1; t < 6; ++t) off[t] = off[t - 1] + cnt[t - 1];
   ctx->nsites = off[5] + cnt[5];
+  if (ctx->nsites == 0) return fail(ctx, HLBG_ERR_INVAL, "geometry has no fluid sites");
   for (int t = 0; t < 6; ++t) ctx->type_count[t] = cnt[t];
   ctx->h_ref2slot.assign((size_t)ctx->nsites, 0);
   for (int64_t rb = 0; rb < nb; ++rb) {

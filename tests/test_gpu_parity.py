@@ -234,6 +234,31 @@ def test_invalid_arguments_fail_loudly():
         s.DoTimeStep(1)  # no initial condition yet
 
 
+def test_empty_and_malformed_geometries_fail_loudly():
+    """No blocks, blocks without a fluid site, a block outside the block grid, a
+    duplicate block and a link record on a solid site: each is refused at
+    creation with a message, never run."""
+    from tests.helpers import ArrayGeometry
+    p = LbmParameters(tau=0.8)
+    one = np.zeros((1, 8), dtype=np.uint64)
+    one[0, 0] = 1  # local site 0 fluid
+    none = np.zeros((0, 8), dtype=np.uint64)
+    empty_rec = ([], [], [], [], [], np.zeros((0, 18)))
+    cases_ = {
+        "no blocks": ArrayGeometry(19, (1, 1, 1), np.zeros((0, 3)), none, *empty_rec),
+        "no fluid sites": ArrayGeometry(19, (1, 1, 1), [[0, 0, 0]], np.zeros((1, 8), np.uint64), *empty_rec),
+        "outside the block grid": ArrayGeometry(19, (1, 1, 1), [[1, 0, 0]], one, *empty_rec),
+        "duplicate block": ArrayGeometry(19, (2, 1, 1), [[0, 0, 0], [0, 0, 0]], np.vstack([one, one]),
+                                         *empty_rec),
+        "solid site": ArrayGeometry(19, (1, 1, 1), [[0, 0, 0]], one, [1], [0], [0], [-1],
+                                    [capi.SITE_FLUID], np.zeros((1, 18))),
+    }
+    for what, g in cases_.items():
+        with pytest.raises(capi.HlbgError) as e:
+            LBM(g.view, p, [], [])
+        assert str(e.value), what
+
+
 @pytest.mark.parametrize("kernel", [capi.KERNEL_LBGK, capi.KERNEL_TRT])
 def test_fluid_list_launch_fp64_bit_exact(kernel):
     """The fluid-list launch (warps of fluid slots only, zero-fill warps for the
