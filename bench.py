@@ -47,7 +47,7 @@ KERNEL_OF_VARIANT = {-1: "k_stream_collide<P, 128, 2>", 0: "k_stream_collide<P, 
                      1: "k_stream_collide<P, 128, 8>", 2: "k_stream_collide<P, 256, 4>",
                      3: "k_stream_collide<P, 512, 2>", 4: "k_stream_collide<P, 128, 10, persistent>",
                      5: "k_stream_collide_listed<P, 128, 9>", 6: "k_stream_collide_listed<P, 128, 8>",
-                     7: "k_stream_collide_staged<128, 8, 4>"}
+                     7: "k_stream_collide_listed<P, 64, 16>"}
 DTYPE = {0: "f64", 1: "f32", 2: "f16-storage/f32"}
 METRIC = "fluid MLUPS (D3Q19 LB update)"
 

@@ -584,15 +584,12 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
   }
 }
 
-// Element stride between directions of one thread in the staged launch's buffer.
-constexpr int kStageStride = 128;
-
 // One warp of the fluid list: 32 fluid sites of one block (or the zero-fill of its
 // solid slots that share sectors with fluid), so no lane is spent on a solid slot.
-template <int P, bool MON, bool STAGED = false>
+template <int P, bool MON>
 __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w,
                                                     const int32_t* __restrict__ block_xyz, MonAccT<P>& acc,
-                                                    bool check, const float* staged = nullptr) {
+                                                    bool check) {
   using St = Store<P>;
   using S = typename St::S;
   using T = typename Calc<P>::T;
@@ -624,13 +621,8 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   if constexpr (MON) uo.load(a, s, check && on);
   T f[Q], fpost[Q];
   if (on) {
-    if constexpr (STAGED) {
 #pragma unroll
-      for (int i = 0; i < Q; ++i) f[i] = staged[i * kStageStride];
-    } else {
-#pragma unroll
-      for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
-    }
+    for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
   } else {
 #pragma unroll
     for (int i = 0; i < Q; ++i) f[i] = (T)(P == 0 ? weight_d(i) : 0.0);
@@ -654,59 +646,6 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   }
 }
 
-// Staged fluid-list launch (FP32 deviations): each warp takes a few consecutive
-// units of the fluid list; while it collides one unit, the 19 values of each lane
-// of its next unit are already on their way into shared memory (cp.async, 4 bytes
-// per lane and direction, lane-private), so loads stay in flight without holding
-// registers.  Shared memory: 2 stages x 19 x THREADS floats.
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_none() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-template <int THREADS>
-__device__ __forceinline__ void stage_unit(const StepArgs& a, int64_t u, float* dst) {
-  if (u >= a.n_warps) return;
-  const int32_t e = __ldg(a.warp_block + u);
-  if (e < 0) return;  // a zero-fill warp reads nothing
-  const unsigned js = __ldg(a.lane_slot + u * 32 + (threadIdx.x & 31));
-  if (js == 0xffffu) return;
-  const float* src = static_cast<const float*>(a.f_old) + (int64_t)e * (Q * kSites) + (js & (kSites - 1));
-#pragma unroll
-  for (int d = 0; d < Q; ++d) cp_async4(dst + d * kStageStride, src + d * kSites);
-}
-
-template <int THREADS, int MINB, int UNITS>
-__global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_staged(StepArgs a, const int32_t* block_xyz) {
-  static_assert(THREADS == kStageStride, "stage layout");
-  __shared__ float buf[2][Q * THREADS];  // [stage][d * THREADS + thread]
-  MonAccF acc = mon_neutral_f();  // unused: the staged launch is not monitored
-  // this warp's UNITS consecutive units of the fluid list (launch order keeps
-  // neighbouring blocks close in time, so their shared sectors merge in L2)
-  const int64_t u0 = ((int64_t)blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5)) * UNITS;
-  stage_unit<THREADS>(a, u0, &buf[0][threadIdx.x]);
-  cp_async_commit();
-#pragma unroll 1
-  for (int k = 0; k < UNITS; ++k) {
-    const int st = k & 1;
-    if (k + 1 < UNITS) stage_unit<THREADS>(a, u0 + k + 1, &buf[st ^ 1][threadIdx.x]);
-    cp_async_commit();
-    cp_async_wait_one();  // this lane's copies of unit u0 + k have landed
-    collide_listed_warp<1, false, true>(a, u0 + k, block_xyz, acc, false, &buf[st][threadIdx.x]);
-  }
-  cp_async_wait_none();
-}
-
-template <int THREADS, int MINB, int UNITS>
-void launch_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
-  const int64_t per_cta = (THREADS / 32) * UNITS;
-  const int64_t g = (a.n_warps + per_cta - 1) / per_cta;
-  if (g > 0) k_stream_collide_staged<THREADS, MINB, UNITS><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
-}
-
 template <int P, int THREADS, int MINB, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArgs a, const int32_t* block_xyz) {
   MonAccT<P> acc = mon_neutral_t<P>();
@@ -721,6 +660,13 @@ void launch_listed(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
   const int64_t g = (a.n_warps * 32 + THREADS - 1) / THREADS;
   if (g) k_stream_collide_listed<P, THREADS, MINB, MON><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
 }
+
+// Fluid-list shape of launch variant 7: 64-thread CTAs, 16 per SM (the 32
+// resident warps of 128 x 8 in smaller CTAs).  Measured on the forest: FP16
+// storage +1% over 128 x 8, FP32 deviations -0.5%; 32-thread CTAs -4%.
+#ifndef HLBG_LISTED7_THREADS
+#define HLBG_LISTED7_THREADS 64
+#endif
 
 // All slots.  THREADS threads per CTA with at least MINB CTAs resident per SM;
 // PERSIST: a grid of resident CTAs striding over 128-slot chunks in order, else
@@ -1253,11 +1199,12 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       return;                                                                                   \
     }                                                                                           \
     if (variant == 7) {                                                                         \
-      if (P == 1 && !a.mon_u) {                                                                 \
-        launch_staged<128, 8, 4>(a, bxyz, st);                                                  \
+      if (!a.mon_u) {                                                                           \
+        launch_listed<P, HLBG_LISTED7_THREADS, (P == 0 ? 2 : 1024 / HLBG_LISTED7_THREADS),      \
+                      false>(a, bxyz, st);                                                      \
         return;                                                                                 \
       }                                                                                         \
-      variant = 6; /* staged only for unmonitored FP32 deviations */                            \
+      variant = 6; /* monitored steps keep 128-thread CTAs (one partial per CTA) */             \
     }                                                                                           \
     if (variant == 6) {                                                                         \
       if (a.mon_u) launch_listed<P, 128, (P == 0 ? 2 : 8), true>(a, bxyz, st);                  \

@@ -288,9 +288,9 @@ int hlbg_incompressibility(hlbg_ctx *ctx, hlbg_incomp *out);
  * the iolets and dominates the time to steady state. */
 int hlbg_average_time_levels(hlbg_ctx *ctx);
 /* Select the stream-and-collide launch shape by index (0..7: 128x10, 128x8, 256x4,
- * 512x2 threads x resident CTAs, a persistent 128x10 grid, the fluid-list launch
- * at 128x9 and 128x8, whose warps hold only fluid slots, and the fluid list with
- * cp.async staging); FP64 runs 128x2 for every index.  No reference counterpart. */
+ * 512x2 threads x resident CTAs, a persistent 128x10 grid, and the fluid-list
+ * launch, whose warps hold only fluid slots, at 128x9, 128x8 and 64x16); FP64 runs
+ * two 128- or 64-thread CTAs per SM.  No reference counterpart. */
 int hlbg_set_launch_variant(hlbg_ctx *ctx, int32_t variant);
 /* Autotuner: time each launch shape / schedule of the stream-and-collide kernel
  * (threads per CTA x resident CTAs per SM, per-slot grid or persistent grid) on
