@@ -586,18 +586,16 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
 
 // One warp of the fluid list: 32 fluid sites of one block (or the zero-fill of its
 // solid slots that share sectors with fluid), so no lane is spent on a solid slot.
+// The unit's list entries (block e, this lane's slot js) are loaded by the caller.
 template <int P, bool MON>
-__device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w,
+__device__ __forceinline__ void collide_listed_unit(const StepArgs& a, int32_t e, unsigned js,
                                                     const int32_t* __restrict__ block_xyz, MonAccT<P>& acc,
                                                     bool check) {
   using St = Store<P>;
   using S = typename St::S;
   using T = typename Calc<P>::T;
-  if (w >= a.n_warps) return;  // whole warp
   const int lane = threadIdx.x & 31;
-  const int32_t e = __ldg(a.warp_block + w);
   const int64_t b = e & 0x7fffffff;
-  const unsigned js = __ldg(a.lane_slot + w * 32 + lane);
   const bool on = js != 0xffffu;
   const int j = on ? (int)(js & (kSites - 1)) : 0;
   const int64_t s = b * kSites + j;
@@ -646,6 +644,15 @@ __device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w
   }
 }
 
+template <int P, bool MON>
+__device__ __forceinline__ void collide_listed_warp(const StepArgs& a, int64_t w,
+                                                    const int32_t* __restrict__ block_xyz, MonAccT<P>& acc,
+                                                    bool check) {
+  if (w >= a.n_warps) return;  // whole warp
+  collide_listed_unit<P, MON>(a, __ldg(a.warp_block + w), __ldg(a.lane_slot + w * 32 + (threadIdx.x & 31)),
+                              block_xyz, acc, check);
+}
+
 template <int P, int THREADS, int MINB, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArgs a, const int32_t* block_xyz) {
   MonAccT<P> acc = mon_neutral_t<P>();
@@ -653,6 +660,45 @@ __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArg
   if constexpr (MON) check = *a.mon_state != 0;
   collide_listed_warp<P, MON>(a, ((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5, block_xyz, acc, check);
   if constexpr (MON) mon_write_partial<P>(a, acc);
+}
+
+// Persistent fluid list: a grid of resident CTAs whose warps stride over the list
+// (warp k takes units k, k + G, k + 2G, ... with G warps in the grid, so the grid
+// still sweeps the list in order), each loading its next unit's entries before it
+// works on the current one, so the index latency overlaps the update.
+template <int P, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
+    k_stream_collide_listed_persist(StepArgs a, const int32_t* block_xyz) {
+  MonAccT<P> acc = mon_neutral_t<P>();  // unused: persistent steps are not monitored
+  const int lane = threadIdx.x & 31;
+  const int64_t G = (int64_t)gridDim.x * (THREADS / 32);
+  int64_t w = ((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5;
+  if (w >= a.n_warps) return;
+  int32_t e = __ldg(a.warp_block + w);
+  unsigned js = __ldg(a.lane_slot + w * 32 + lane);
+  for (; w < a.n_warps; w += G) {
+    const int64_t wn = w + G;
+    int32_t en = 0;
+    unsigned jsn = 0xffffu;
+    if (wn < a.n_warps) {
+      en = __ldg(a.warp_block + wn);
+      jsn = __ldg(a.lane_slot + wn * 32 + lane);
+    }
+    collide_listed_unit<P, false>(a, e, js, block_xyz, acc, false);
+    e = en;
+    js = jsn;
+  }
+}
+
+template <int P, int THREADS, int MINB>
+void launch_listed_persist(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // MINB CTAs per SM are resident by the launch bounds (no shared memory)
+  const int64_t need = (a.n_warps * 32 + THREADS - 1) / THREADS;
+  const int64_t g = std::min<int64_t>(need, (int64_t)sms * MINB);
+  if (g > 0) k_stream_collide_listed_persist<P, THREADS, MINB><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
 }
 
 template <int P, int THREADS, int MINB, bool MON>
@@ -668,22 +714,15 @@ void launch_listed(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
 #define HLBG_LISTED7_THREADS 64
 #endif
 
-// All slots.  THREADS threads per CTA with at least MINB CTAs resident per SM;
-// PERSIST: a grid of resident CTAs striding over 128-slot chunks in order, else
-// one thread per slot.  The variants are the autotuner's candidates.
-template <int P, int THREADS, int MINB, bool PERSIST, bool MON>
+// All slots, one thread per slot: THREADS threads per CTA with at least MINB CTAs
+// resident per SM.  The shapes are the autotuner's candidates.
+template <int P, int THREADS, int MINB, bool MON>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_stream_collide(StepArgs a, const int32_t* block_xyz) {
   MonAccT<P> acc = mon_neutral_t<P>();
   bool check = false;
   if constexpr (MON) check = *a.mon_state != 0;
-  if constexpr (!PERSIST) {
-    collide_slot<P, MON>(a, (int64_t)blockIdx.x * THREADS + threadIdx.x, block_xyz, acc, check);
-  } else {
-    const int64_t nchunk = a.nslot / THREADS;
-    for (int64_t c = blockIdx.x; c < nchunk; c += gridDim.x)
-      collide_slot<P, MON>(a, c * THREADS + threadIdx.x, block_xyz, acc, check);
-  }
+  collide_slot<P, MON>(a, (int64_t)blockIdx.x * THREADS + threadIdx.x, block_xyz, acc, check);
   if constexpr (MON) mon_write_partial<P>(a, acc);
 }
 
@@ -1164,21 +1203,10 @@ __global__ void __launch_bounds__(256) k_average(AverageArgs aa) {
 }  // namespace hlbg
 
 namespace hlbg {
-template <int P, int THREADS, int MINB, bool PERSIST, bool MON = false>
+template <int P, int THREADS, int MINB, bool MON = false>
 void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
-  unsigned g;
-  if constexpr (PERSIST) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream_collide<P, THREADS, MINB, PERSIST, MON>,
-                                                  THREADS, 0);
-    const int64_t chunks = a.nslot / THREADS;
-    g = (unsigned)std::min<int64_t>(chunks, (int64_t)sms * std::max(per_sm, 1));
-  } else {
-    g = (unsigned)(a.nslot / THREADS);
-  }
-  if (g) k_stream_collide<P, THREADS, MINB, PERSIST, MON><<<g, THREADS, 0, st>>>(a, bxyz);
+  const unsigned g = (unsigned)(a.nslot / THREADS);
+  if (g) k_stream_collide<P, THREADS, MINB, MON><<<g, THREADS, 0, st>>>(a, bxyz);
 }
 }  // namespace hlbg
 
@@ -1191,9 +1219,14 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       if (g) k_stream_collide_list<P><<<g, 256, 0, st>>>(a, bxyz);                              \
       return;                                                                                   \
     }                                                                                           \
-    /* monitored steps carry more live values: the 10-CTA shapes become 8-CTA ones */            \
-    if (a.mon_u && (variant == 0 || variant == 4)) variant = 1;                                  \
-    if (a.mon_u && variant == 5) variant = 6;                                                   \
+    /* monitored steps: the 10-CTA all-slots shape becomes 128 x 8, every fluid-list    */      \
+    /* shape the 128 x 8 fluid list (one partial per 128-thread CTA)                     */      \
+    if (a.mon_u && variant == 0) variant = 1;                                                   \
+    if (a.mon_u && variant >= 4) variant = 6;                                                   \
+    if (variant == 4) {                                                                         \
+      launch_listed_persist<P, 128, (P == 0 ? 2 : 8)>(a, bxyz, st);                             \
+      return;                                                                                   \
+    }                                                                                           \
     if (variant == 5) {                                                                         \
       launch_listed<P, 128, (P == 0 ? 2 : 9), false>(a, bxyz, st);                              \
       return;                                                                                   \
@@ -1212,26 +1245,25 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
       return;                                                                                   \
     }                                                                                           \
     if (P == 0) variant = -1;                                                                   \
-    if (a.mon_u) { /* one partial per CTA: the persistent shape is not used */                  \
+    if (a.mon_u) { /* one partial per CTA */                                                    \
       switch (variant) {                                                                        \
-        case 2: launch_sc<P, 256, (P == 0 ? 2 : 4), false, true>(a, bxyz, st); break;           \
-        case 3: launch_sc<P, 512, (P == 0 ? 1 : 2), false, true>(a, bxyz, st); break;           \
-        case -1: launch_sc<P, 128, 2, false, true>(a, bxyz, st); break;                         \
-        default: launch_sc<P, 128, (P == 0 ? 2 : 8), false, true>(a, bxyz, st); break;          \
+        case 2: launch_sc<P, 256, (P == 0 ? 2 : 4), true>(a, bxyz, st); break;                  \
+        case 3: launch_sc<P, 512, (P == 0 ? 1 : 2), true>(a, bxyz, st); break;                  \
+        case -1: launch_sc<P, 128, 2, true>(a, bxyz, st); break;                                \
+        default: launch_sc<P, 128, (P == 0 ? 2 : 8), true>(a, bxyz, st); break;                 \
       }                                                                                         \
       return;                                                                                   \
     }                                                                                           \
     switch (variant) {                                                                          \
-      case 1: launch_sc<P, 128, (P == 0 ? 2 : 8), false>(a, bxyz, st); break;                   \
-      case 2: launch_sc<P, 256, (P == 0 ? 2 : 4), false>(a, bxyz, st); break;                   \
-      case 3: launch_sc<P, 512, (P == 0 ? 1 : 2), false>(a, bxyz, st); break;                   \
-      case 4: launch_sc<P, 128, (P == 0 ? 2 : 10), true>(a, bxyz, st); break;                   \
-      case -1: launch_sc<P, 128, 2, false>(a, bxyz, st); break;                                 \
-      default: launch_sc<P, HLBG_SC_THREADS, HLBG_SC_MINB, false>(a, bxyz, st); break;          \
+      case 1: launch_sc<P, 128, (P == 0 ? 2 : 8)>(a, bxyz, st); break;                          \
+      case 2: launch_sc<P, 256, (P == 0 ? 2 : 4)>(a, bxyz, st); break;                          \
+      case 3: launch_sc<P, 512, (P == 0 ? 1 : 2)>(a, bxyz, st); break;                          \
+      case -1: launch_sc<P, 128, 2>(a, bxyz, st); break;                                        \
+      default: launch_sc<P, HLBG_SC_THREADS, HLBG_SC_MINB>(a, bxyz, st); break;                 \
     }                                                                                           \
   }                                                                                             \
   int64_t monitored_grid_##P(int64_t nslot, int variant, int64_t n_warps) {                    \
-    if (variant >= 5) return (n_warps * 32 + 127) / 128; /* monitored 7 runs as 6 */            \
+    if (variant >= 4) return (n_warps * 32 + 127) / 128; /* monitored 4..7 run as 6 */          \
     if (P == 0) return nslot / 128;                                                             \
     switch (variant) {                                                                          \
       case 1: return nslot / 128;                                                               \
