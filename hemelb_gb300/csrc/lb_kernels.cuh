@@ -329,13 +329,14 @@ __device__ __forceinline__ MonAcc mon_block(MonAcc v) {
   return v;
 }
 
-// The FP32 forms accumulate their per-thread monitor values in FP32 (min / max are
-// exact in any precision; the mass as a count plus the sum of the density
-// deviations, which are small) and switch to FP64 only for each warp's result:
-// GB300's FP64 rate would otherwise make every monitored site an FP64 workload.
+// The FP32 forms accumulate their monitor values in FP32 and integers up to the
+// CTA's partial (min / max are exact in any precision; the mass is a count plus
+// the sum of the density deviations, which are small); only the second reduction
+// stage works in FP64: GB300's FP64 rate would otherwise make every monitored CTA
+// an FP64 workload.
 struct MonAccF {
-  float dm, maxdu, minf, dmin, dmax, umax;  // dm: sum of rho - 1; dmin/dmax: of rho - 1
-  unsigned count, bad;
+  float dm, maxdu, minf, dmin, dmax, umax;  // dm: sum of rho - 1; dmin/dmax: of rho - 1;
+  unsigned count, bad;                      // maxdu, umax: squared (see mon_site)
 };
 __device__ __forceinline__ MonAccF mon_neutral_f() {
   return MonAccF{0.f, 0.f, 1.0e30f, 1.0e30f, -1.0e30f, 0.f, 0u, 0u};
@@ -437,22 +438,21 @@ __device__ __forceinline__ void mon_site(const StepArgs& a, int64_t s, const flo
   const float ir = 1.f / (1.f + m0);
   const float ux = mx * ir, uy = my * ir, uz = mz * ir;
   if (check) {
+    // |du| and |u| are kept squared until the CTA's partial is written (the square
+    // root is monotonic, so the maximum is the same)
     const float dx = ux - uo.x, dy = uy - uo.y, dz = uz - uo.z;
-    const float du = sqrtf(dx * dx + dy * dy + dz * dz);
-    if (!(du <= acc.maxdu)) acc.maxdu = du;
+    const float du2 = dx * dx + dy * dy + dz * dz;
+    if (!(du2 <= acc.maxdu)) acc.maxdu = du2;
     acc.dm += m0;
     acc.dmin = fminf(acc.dmin, m0);
     acc.dmax = fmaxf(acc.dmax, m0);
-    const float um = sqrtf(ux * ux + uy * uy + uz * uz);
-    if (!(um <= acc.umax)) acc.umax = um;
-    bool bad = false;
+    const float um2 = ux * ux + uy * uy + uz * uz;
+    if (!(um2 <= acc.umax)) acc.umax = um2;
     float mn = 1.0e30f;
 #pragma unroll
-    for (int d = 0; d < Q; ++d) {
-      const float fv = f[d] + weight_f(d);
-      bad |= !(fv > 0.f);
-      mn = fminf(mn, fv);
-    }
+    for (int d = 0; d < Q; ++d) mn = fminf(mn, f[d] + weight_f(d));
+    // some f <= 0, or a NaN among them (which fminf skips but the density sum keeps)
+    const bool bad = !(mn > 0.f) || m0 != m0;
     acc.minf = fminf(acc.minf, mn);
     acc.bad += bad ? 1u : 0u;
     acc.count += 1u;
@@ -491,11 +491,11 @@ __device__ __forceinline__ void mon_write_partial(const StepArgs& a, const MonAc
     if (threadIdx.x == 0) {
       float* p = reinterpret_cast<float*>(a.mon_part);
       p[blockIdx.x] = r.dm;
-      p[n + blockIdx.x] = r.maxdu;
+      p[n + blockIdx.x] = sqrtf(r.maxdu);
       p[2 * n + blockIdx.x] = r.minf;
       p[3 * n + blockIdx.x] = r.dmin;
       p[4 * n + blockIdx.x] = r.dmax;
-      p[5 * n + blockIdx.x] = r.umax;
+      p[5 * n + blockIdx.x] = sqrtf(r.umax);
       p[6 * n + blockIdx.x] = __uint_as_float(r.count);
       p[7 * n + blockIdx.x] = __uint_as_float(r.bad);
     }
