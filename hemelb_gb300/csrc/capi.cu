@@ -38,6 +38,32 @@ const int HCY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -
 const int HCZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
 const int HINV[19] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
 
+// Device block order (HLBG_BLOCK_SORT): 0 z-columns in 2-D Morton order of (x, y);
+// 1 3-D Morton order; 2 z-columns along a 2-D Hilbert curve of (x, y).
+#ifndef HLBG_BLOCK_SORT
+#define HLBG_BLOCK_SORT 0
+#endif
+
+// Index of (x, y) along a 2-D Hilbert curve over an n x n grid (n a power of two):
+// the standard rotate-and-reflect walk from the top quadrant down.
+uint64_t hilbert2(uint32_t n, uint32_t x, uint32_t y) {
+  uint64_t d = 0;
+  for (uint32_t s = n / 2; s > 0; s /= 2) {
+    const uint32_t rx = (x & s) ? 1u : 0u, ry = (y & s) ? 1u : 0u;
+    d += (uint64_t)s * s * ((3u * rx) ^ ry);
+    if (ry == 0) {
+      if (rx == 1) {  // reflect (only the bits below s matter from here on)
+        x = n - 1 - x;
+        y = n - 1 - y;
+      }
+      const uint32_t t = x;
+      x = y;
+      y = t;
+    }
+  }
+  return d;
+}
+
 uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
   uint64_t m = 0;
   for (int k = 0; k < 16; ++k) {
@@ -359,13 +385,22 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   // writers of every z-shifted row of a push are z-adjacent blocks; running them
   // back to back lets their partial 32-byte sectors merge in L2.  The reference's
   // own numbering (3-D Morton order) is kept separately in ref_rank below.
+  uint32_t hn = 1;  // Hilbert grid side: a power of two covering the block grid
+  while (hn < (uint32_t)std::max(NX, NY)) hn *= 2;
+  (void)hn;
   std::vector<std::pair<uint64_t, int64_t>> order((size_t)nb);
   std::vector<std::pair<uint64_t, int64_t>> ref_order((size_t)nb);
   for (int64_t b = 0; b < nb; ++b) {
     int32_t x = g->block_coords[3 * b], y = g->block_coords[3 * b + 1], z = g->block_coords[3 * b + 2];
     if (x < 0 || y < 0 || z < 0 || x >= NX || y >= NY || z >= NZ)
       return fail(ctx, HLBG_ERR_INVAL, "block coordinate outside the block grid");
+#if HLBG_BLOCK_SORT == 1
+    order[b] = {morton3(x, y, z), b};
+#elif HLBG_BLOCK_SORT == 2
+    order[b] = {(hilbert2(hn, x, y) << 16) | (uint64_t)z, b};
+#else
     order[b] = {(morton3(x, y, 0) << 16) | (uint64_t)z, b};
+#endif
     ref_order[b] = {morton3(x, y, z), b};
   }
   std::sort(order.begin(), order.end());
