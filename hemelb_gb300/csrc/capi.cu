@@ -129,6 +129,10 @@ struct hlbg_ctx {
   int32_t* d_warp_block = nullptr;  // fluid-list launch (StepArgs::warp_block)
   uint16_t* d_lane_slot = nullptr;
   int64_t n_warps = 0;
+  std::vector<int32_t> h_flux_slot, h_flux_gi;  // sites with iolet links, their iolet
+  int32_t* d_flux_slot = nullptr;
+  int32_t* d_flux_gi = nullptr;
+  double* d_flux = nullptr;
   uint16_t* d_slot2site = nullptr;  // packed blocks: local site of each slot
   uint16_t* d_site2slot = nullptr;  // packed blocks: slot of each local site
   std::vector<uint16_t> h_slot2site;
@@ -640,6 +644,14 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     code.swap(pc);
   }
   for (auto& v : ctx->h_rec_slot) v = (int32_t)slot_of(v);
+  // sites with links to an iolet, for hlbg_iolet_flux (record order)
+  for (size_t r = 0; r < rtype.size(); ++r) {
+    const int t = rtype[r];
+    if (t < 2 || t > 5 || rid[r] < 0) continue;
+    const bool inlet = (t == 2 || t == 4);
+    ctx->h_flux_slot.push_back(ctx->h_rec_slot[r]);
+    ctx->h_flux_gi.push_back(inlet ? rid[r] : (int32_t)ctx->inlets.size() + rid[r]);
+  }
   for (auto& v : ctx->h_ref2slot) v = (int32_t)slot_of(v);
   for (auto& v : ctx->h_ps_slot) v = (int32_t)slot_of(v);
   for (auto& e : bnbr)
@@ -689,6 +701,8 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   if ((rc = upload(ctx, &ctx->d_b_wall, rw))) return rc;
   if ((rc = upload(ctx, &ctx->d_b_iolet, ri))) return rc;
   if ((rc = upload(ctx, &ctx->d_b_ioid, rid))) return rc;
+  if ((rc = upload(ctx, &ctx->d_flux_slot, ctx->h_flux_slot))) return rc;
+  if ((rc = upload(ctx, &ctx->d_flux_gi, ctx->h_flux_gi))) return rc;
   if ((rc = upload(ctx, &ctx->d_b_type, rtype))) return rc;
   if (want_cut && (rc = upload(ctx, &ctx->d_b_cut, rcut))) return rc;
   if ((rc = upload(ctx, &ctx->d_b_links, rlinks))) return rc;
@@ -880,7 +894,8 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_list,      ctx->d_part,      ctx->d_part_bad,  ctx->d_steady,
                   ctx->d_steady_n,  ctx->d_slot2site, ctx->d_site2slot, ctx->d_mon_u,
                   ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result,
-                  ctx->d_warp_block, ctx->d_lane_slot, ctx->d_b_normal, ctx->d_wss};
+                  ctx->d_warp_block, ctx->d_lane_slot, ctx->d_b_normal, ctx->d_wss,
+                  ctx->d_flux_slot, ctx->d_flux_gi, ctx->d_flux};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
@@ -1493,6 +1508,40 @@ int hlbg_wall_shear_stress(hlbg_ctx* ctx, double* out) {
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, ctx->d_wss, sizeof(double) * ctx->nsites, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return HLBG_OK;
+}
+
+int hlbg_iolet_flux(hlbg_ctx* ctx, double* out, int32_t n) {
+  if (!ctx || (!out && n > 0)) return HLBG_ERR_INVAL;
+  const int32_t nio = (int32_t)(ctx->inlets.size() + ctx->outlets.size());
+  if (n != nio) return fail(ctx, HLBG_ERR_INVAL, "flux array must hold one value per inlet and outlet");
+  if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
+  const int64_t m = (int64_t)ctx->h_flux_slot.size();
+  std::vector<double> per(m);
+  if (m > 0) {
+    if (!ctx->d_flux) {
+      int rc = dev_alloc(ctx, &ctx->d_flux, (size_t)m);
+      if (rc) return rc;
+    }
+    FluxArgs fa{};
+    fa.f = ctx->f[ctx->cur];
+    fa.slot = ctx->d_flux_slot;
+    fa.gi = ctx->d_flux_gi;
+    fa.iolets = ctx->d_iolets;
+    fa.count = m;
+    fa.out = ctx->d_flux;
+    fa.fp16_inv_scale = 1.0f / ctx->fp16_scale;
+    switch (ctx->prec) {
+      case 0: launch_flux_0(fa, ctx->stream); break;
+      case 1: launch_flux_1(fa, ctx->stream); break;
+      default: launch_flux_2(fa, ctx->stream); break;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(per.data(), ctx->d_flux, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  for (int32_t k = 0; k < n; ++k) out[k] = 0.0;
+  for (int64_t i = 0; i < m; ++i) out[ctx->h_flux_gi[i]] += per[i];  // fixed order
   return HLBG_OK;
 }
 

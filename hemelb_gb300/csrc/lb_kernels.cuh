@@ -1109,6 +1109,36 @@ static __global__ void __launch_bounds__(256) k_monitor_final(MonitorArgs ma, in
 
 // Lattice::CalculateWallShearStressMagnitude (Code/lb/lattices/Lattice.h:652-686)
 // with CalculatePiTensor (:696-726) on f_neq = f - f_eq of the state, as
+// Mass flux through the iolets: for every site with links to iolet gi, its
+// momentum sum_d c_d f_d (the reference's CalculateDensityAndMomentum order) along
+// the iolet's normalised inward normal, in FP64.  No reference counterpart: the
+// host sums the per-site values of each iolet in list order.
+template <int P>
+__global__ void k_iolet_flux(FluxArgs fa) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= fa.count) return;
+  const int64_t s = fa.slot[i];
+  const int64_t off = fidx(s, 0);
+  double mx = 0.0, my = 0.0, mz = 0.0;
+#pragma unroll
+  for (int d = 0; d < Q; ++d) {
+    double fd;
+    if constexpr (P == 0) {
+      fd = static_cast<const double*>(fa.f)[off + d * kSites];
+    } else if constexpr (P == 1) {
+      fd = (double)static_cast<const float*>(fa.f)[off + d * kSites] + weight_d(d);
+    } else {
+      fd = (double)(__half2float(static_cast<const __half*>(fa.f)[off + d * kSites]) * fa.fp16_inv_scale) +
+           weight_d(d);
+    }
+    mx += (double)Lat::cx(d) * fd;
+    my += (double)Lat::cy(d) * fd;
+    mz += (double)Lat::cz(d) * fd;
+  }
+  const IoletDev& io = fa.iolets[fa.gi[i]];
+  fa.out[i] = dot3d(mx, my, mz, io.n[0], io.n[1], io.n[2]);
+}
+
 // UpdateCachePostCollision fills wallShearStressMagnitudeCache
 // (Code/lb/streamers/Common.h:35-52): FP64 and the reference's operation order.
 template <int P>
@@ -1317,6 +1347,10 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
   void launch_wss_##P(const WssArgs& wa, cudaStream_t st) {                                     \
     unsigned g = (unsigned)((wa.count + 255) / 256);                                            \
     if (g) k_wss<P><<<g, 256, 0, st>>>(wa);                                                     \
+  }                                                                                             \
+  void launch_flux_##P(const FluxArgs& fa, cudaStream_t st) {                                   \
+    unsigned g = (unsigned)((fa.count + 255) / 256);                                            \
+    if (g) k_iolet_flux<P><<<g, 256, 0, st>>>(fa);                                              \
   }                                                                                             \
   void launch_average_##P(const AverageArgs& aa, cudaStream_t st) {                             \
     unsigned g = (unsigned)((aa.nslot + 255) / 256);                                            \

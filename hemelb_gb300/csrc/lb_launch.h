@@ -105,6 +105,18 @@ struct WssArgs {
   float fp16_inv_scale;
 };
 
+// Mass flux through each iolet: per listed site (a site with links to that
+// iolet) its momentum along the iolet's inward normal.
+struct FluxArgs {
+  const void* f;
+  const int32_t* slot;  // [count]
+  const int32_t* gi;    // [count] inlets first, then outlets
+  const IoletDev* iolets;
+  int64_t count;
+  double* out;  // [count]
+  float fp16_inv_scale;
+};
+
 #define HLBG_DECLARE(P)                                                              \
   void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st,  \
                                  int variant);                                           \
@@ -122,7 +134,8 @@ struct WssArgs {
                              int32_t* mon_state, double* result, const SteadyArgs& sa,        \
                              int steady, cudaStream_t st);                                     \
   void launch_average_##P(const AverageArgs& aa, cudaStream_t st);                    \
-  void launch_wss_##P(const WssArgs& wa, cudaStream_t st);
+  void launch_wss_##P(const WssArgs& wa, cudaStream_t st);                                \
+  void launch_flux_##P(const FluxArgs& fa, cudaStream_t st);
 
 HLBG_DECLARE(0)
 HLBG_DECLARE(1)

@@ -236,6 +236,7 @@ class LBM:
         self._geom_keep = geometry
         gview = geometry.view if isinstance(geometry, SyntheticGeometry) else geometry
         ni, no = len(inlets), len(outlets)
+        self._n_inlets, self._n_outlets = ni, no
         self._inl = (capi.Iolet * max(ni, 1))(*inlets)
         self._outl = (capi.Iolet * max(no, 1))(*outlets)
         pc = params.to_c()
@@ -349,6 +350,14 @@ class LBM:
         """Wall shear stress magnitude per contiguous site (float max where no wall link)."""
         out = np.empty(self.n_sites, dtype=np.float64)
         check(self._lib.hlbg_wall_shear_stress(self._ctx, out.ctypes.data_as(_D)), self._ctx)
+        return out
+
+    def IoletFlux(self) -> np.ndarray:
+        """Mass flux through each iolet (inlets, then outlets) of the current state:
+        momentum of the sites with links to it along its inward normal."""
+        n = self._n_inlets + self._n_outlets
+        out = np.zeros(n, dtype=np.float64)
+        check(self._lib.hlbg_iolet_flux(self._ctx, out.ctypes.data_as(_D), n), self._ctx)
         return out
 
     def Incompressibility(self) -> capi.Incomp:

@@ -252,6 +252,13 @@ int hlbg_run_to_steady(hlbg_ctx *ctx, double tol, double u_ref, int64_t max_step
  * Replaces hlbg_step + hlbg_reduce per step without re-reading both arrays
  * (Code/lb/StabilityTester.h:91-183). */
 int hlbg_step_monitored(hlbg_ctx *ctx, int32_t nsteps, hlbg_stats *out);
+/* Mass flux through each iolet of the current state: out[k] (inlets first, then
+ * outlets; n = their total) sums, over the sites with links to that iolet, the
+ * site's momentum sum_d c_d f_d along the iolet's normalised inward normal, in
+ * FP64, in a fixed order.  Inflow is positive at inlets and negative at outlets;
+ * at steady state the sum over all iolets is ~0.  No reference counterpart (the
+ * per-iolet flux of the monitoring reductions). */
+int hlbg_iolet_flux(hlbg_ctx *ctx, double *out, int32_t n);
 /* XTR distribution checkpoints (doc/dev/file-formats/extraction.md, version 5): one
  * field "distributions" of 19 doubles per site, sites in contiguous order with their
  * grid positions, one record per timestep, and the ".off" offset file of a single

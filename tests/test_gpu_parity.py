@@ -363,3 +363,56 @@ def test_wall_shear_stress_matches_reference_formula():
     assert np.all(np.abs(got - exp) <= 1e-12 * np.abs(exp).max())
     assert np.all(w[~wall] == np.finfo(np.float64).max)
     assert exp.max() > 0
+
+
+def _flux_reference(o, g, n_in, iolets):
+    """Per-iolet sum over the sites with iolet links of their momentum along the
+    iolet's normalised normal, from the oracle's state (FP64 numpy)."""
+    from tests.helpers import CX19, CY19, CZ19
+    a = o.arrays()
+    f = o.fold()
+    c = np.array([CX19, CY19, CZ19], dtype=np.float64)  # (3, 19)
+    rec = {int(ls): k for k, ls in enumerate(g.link_site)}
+    out = np.zeros(len(iolets))
+    scale = np.zeros(len(iolets))
+    for i in np.nonzero(a["iolet_mask"] != 0)[0]:
+        k = rec[int(a["slot"][i])]
+        gi = int(a["iolet_id"][i]) + (0 if g.site_type[k] == capi.SITE_INLET else n_in)
+        nrm = np.array(iolets[gi].normal[:], dtype=np.float64)
+        v = float((c @ f[i]) @ (nrm / np.sqrt(nrm @ nrm)))
+        out[gi] += v
+        scale[gi] += abs(v)
+    return out, scale
+
+
+@pytest.mark.parametrize("case", ["pipe", "bifurcation"])
+def test_iolet_flux_matches_oracle_state(case):
+    """Mass flux per iolet (momentum along the inward normal over the sites with
+    links to it) of the FP64 state against the same sum on the oracle's state."""
+    c = cases.pipe() if case == "pipe" else small_bifurcation(seed=4)
+    o = oracle_for(c)
+    o.step(200, THREADS)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(200)
+    got = s.IoletFlux()
+    exp, scale = _flux_reference(o, c.geometry, len(c.inlets), list(c.inlets) + list(c.outlets))
+    assert len(got) == len(c.inlets) + len(c.outlets)
+    assert np.all(scale > 0)
+    assert np.all(np.abs(got - exp) <= 1e-12 * scale)
+    import ctypes as C
+    short = np.zeros(1)  # one value for two or more iolets
+    assert s._lib.hlbg_iolet_flux(s.ctx, short.ctypes.data_as(C.POINTER(C.c_double)), 1) == capi.HLBG_ERR_INVAL
+
+
+def test_iolet_flux_balances_at_steady_state():
+    """Pipe run to the StabilityTester's steady state: the flux in at the inlet
+    equals the flux out at the outlet (mass conservation) to 1e-4."""
+    c = cases.pipe()
+    s = c.solver()
+    s.SetInitialConditions()
+    first, run, du, rc = s.RunToSteady(1e-6, 0.01, max_steps=50000)
+    assert rc == capi.HLBG_OK
+    phi_in, phi_out = s.IoletFlux()
+    assert phi_in > 0 and phi_out < 0
+    assert abs(phi_in + phi_out) <= 1e-4 * phi_in
