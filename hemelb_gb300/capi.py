@@ -114,6 +114,7 @@ SIGNATURES = {
     "hlbg_incompressibility": (C.c_int, [C.c_void_p, C.POINTER(Incomp)]),
     "hlbg_wall_shear_stress": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_iolet_flux": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
+    "hlbg_set_iolets": (C.c_int, [C.c_void_p, C.POINTER(Iolet), C.c_int32, C.POINTER(Iolet), C.c_int32]),
     "hlbg_write_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_uint64, C.c_double,
                                         C.POINTER(C.c_double), C.c_int32]),
     "hlbg_read_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64, C.POINTER(C.c_uint64)]),

@@ -877,7 +877,72 @@ int graph_steps(hlbg_ctx* ctx, int n, bool check) {
 
 }  // namespace
 
+namespace {
+
+// Iolet parameters of a context: the models must match the streamers (Nash reads
+// a density, Ladd a velocity), and the warm-up start density is the smallest iolet
+// density (LBM::PrepareBoundaryObjects, Code/lb/lb.hpp:127-152).
+int set_iolet_params(hlbg_ctx* ctx, const hlbg_iolet* inlets, int32_t n_inlets, const hlbg_iolet* outlets,
+                     int32_t n_outlets) {
+  const hlbg_params* p = &ctx->params;
+  for (int32_t k = 0; k < n_inlets; ++k)
+    if ((p->inlet == HLBG_IOLET_NASH) != (inlets[k].model == HLBG_IOLET_COSINE))
+      return fail(ctx, HLBG_ERR_INVAL, "inlet model does not match the inlet streamer");
+  for (int32_t k = 0; k < n_outlets; ++k)
+    if ((p->outlet == HLBG_IOLET_NASH) != (outlets[k].model == HLBG_IOLET_COSINE))
+      return fail(ctx, HLBG_ERR_INVAL, "outlet model does not match the outlet streamer");
+  ctx->inlets.assign(inlets, inlets + n_inlets);
+  ctx->outlets.assign(outlets, outlets + n_outlets);
+  double mind = 1.7976931348623157e308;
+  for (auto* v : {&ctx->inlets, &ctx->outlets})
+    for (auto& io : *v) {
+      double dm = io.model == HLBG_IOLET_COSINE ? io.density_mean - io.density_amp : 1.0;
+      mind = std::min(mind, dm);
+    }
+  ctx->min_density = mind;
+  return HLBG_OK;
+}
+
+// Device copy of the iolets' geometry: position, normal normalised
+// (InOutLet::SetNormal) and rounded to float as the Nash link reads it, radius, model.
+std::vector<IoletDev> iolet_table(const hlbg_ctx* ctx) {
+  std::vector<IoletDev> iod;
+  for (auto* v : {&ctx->inlets, &ctx->outlets})
+    for (auto& io : *v) {
+      IoletDev d{};
+      double mag = std::sqrt(dot3(io.normal, io.normal));
+      for (int k = 0; k < 3; ++k) {
+        d.pos[k] = io.position[k];
+        d.n[k] = io.normal[k] / mag;
+        d.nf[k] = (double)(float)d.n[k];
+      }
+      d.radius = io.radius;
+      d.model = io.model;
+      iod.push_back(d);
+    }
+  return iod;
+}
+
+}  // namespace
+
 extern "C" {
+
+int hlbg_set_iolets(hlbg_ctx* ctx, const hlbg_iolet* inlets, int32_t n_inlets, const hlbg_iolet* outlets,
+                    int32_t n_outlets) {
+  if (!ctx || (n_inlets && !inlets) || (n_outlets && !outlets)) return HLBG_ERR_INVAL;
+  if (n_inlets != (int32_t)ctx->inlets.size() || n_outlets != (int32_t)ctx->outlets.size())
+    return fail(ctx, HLBG_ERR_INVAL, "the geometry's iolet counts cannot change");
+  // the previous step's iolet values must have been copied before they change
+  CK(cudaStreamSynchronize(ctx->stream));
+  int rc = set_iolet_params(ctx, inlets, n_inlets, outlets, n_outlets);
+  if (rc) return rc;
+  const std::vector<IoletDev> iod = iolet_table(ctx);
+  if (!iod.empty())
+    CK(cudaMemcpy(ctx->d_iolets, iod.data(), iod.size() * sizeof(IoletDev), cudaMemcpyHostToDevice));
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);  // captured iolet values changed
+  ctx->graphs.clear();
+  return HLBG_OK;
+}
 
 const char* hlbg_version(void) { return "hemelb_gb300 0.1 (sm_103a, D3Q19)"; }
 
@@ -934,47 +999,17 @@ int hlbg_create(const hlbg_geometry* g, const hlbg_params* p, const hlbg_iolet* 
   ctx->params = *p;
   ctx->prec = p->precision;
   ctx->elem = p->precision == HLBG_FP64 ? 8 : (p->precision == HLBG_FP32DEV ? 4 : 2);
-  ctx->inlets.assign(inlets, inlets + n_inlets);
-  ctx->outlets.assign(outlets, outlets + n_outlets);
-  // iolet models must match the streamer: Nash reads a density, Ladd a velocity
-  for (auto& io : ctx->inlets)
-    if ((p->inlet == HLBG_IOLET_NASH) != (io.model == HLBG_IOLET_COSINE))
-      return fail(ctx, HLBG_ERR_INVAL, "inlet model does not match the inlet streamer");
-  for (auto& io : ctx->outlets)
-    if ((p->outlet == HLBG_IOLET_NASH) != (io.model == HLBG_IOLET_COSINE))
-      return fail(ctx, HLBG_ERR_INVAL, "outlet model does not match the outlet streamer");
-  // LBM::PrepareBoundaryObjects (Code/lb/lb.hpp:127-152)
-  double mind = 1.7976931348623157e308;
-  for (auto* v : {&ctx->inlets, &ctx->outlets})
-    for (auto& io : *v) {
-      double dm = io.model == HLBG_IOLET_COSINE ? io.density_mean - io.density_amp : 1.0;
-      mind = std::min(mind, dm);
-    }
-  ctx->min_density = mind;
+  int rc = set_iolet_params(ctx, inlets, n_inlets, outlets, n_outlets);
+  if (rc) return rc;
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&ctx->ev0));
   CK(cudaEventCreate(&ctx->ev1));
   CK(cudaEventCreateWithFlags(&ctx->io_copied, cudaEventDisableTiming));
   CK(cudaEventRecord(ctx->io_copied, ctx->stream));
-  int rc = build_layout(ctx, g);
-  if (rc) return rc;
+  if ((rc = build_layout(ctx, g))) return rc;
   // iolet constants
   ctx->n_io = (int)(ctx->inlets.size() + ctx->outlets.size());
-  std::vector<IoletDev> iod;
-  for (auto* v : {&ctx->inlets, &ctx->outlets})
-    for (auto& io : *v) {
-      IoletDev d{};
-      double mag = std::sqrt(dot3(io.normal, io.normal));  // InOutLet::SetNormal
-      for (int k = 0; k < 3; ++k) {
-        d.pos[k] = io.position[k];
-        d.n[k] = io.normal[k] / mag;
-        d.nf[k] = (double)(float)d.n[k];
-      }
-      d.radius = io.radius;
-      d.model = io.model;
-      iod.push_back(d);
-    }
-  if ((rc = upload(ctx, &ctx->d_iolets, iod))) return rc;
+  if ((rc = upload(ctx, &ctx->d_iolets, iolet_table(ctx)))) return rc;
   if (ctx->n_io) {
     if ((rc = dev_alloc(ctx, &ctx->d_io_tab, (size_t)kStepBatch * 2 * ctx->n_io))) return rc;
     CK(cudaMallocHost((void**)&ctx->h_io_tab, sizeof(double) * kStepBatch * 2 * ctx->n_io));

@@ -352,6 +352,13 @@ class LBM:
         check(self._lib.hlbg_wall_shear_stress(self._ctx, out.ctypes.data_as(_D)), self._ctx)
         return out
 
+    def SetIolets(self, inlets, outlets):
+        """New iolet parameters (same counts as at creation)."""
+        ni, no = len(inlets), len(outlets)
+        self._inl = (capi.Iolet * max(ni, 1))(*inlets)
+        self._outl = (capi.Iolet * max(no, 1))(*outlets)
+        check(self._lib.hlbg_set_iolets(self._ctx, self._inl, ni, self._outl, no), self._ctx)
+
     def IoletFlux(self) -> np.ndarray:
         """Mass flux through each iolet (inlets, then outlets) of the current state:
         momentum of the sites with links to it along its inward normal."""

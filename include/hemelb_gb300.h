@@ -200,6 +200,12 @@ void hlbg_synth_free(void *geom_handle);
 int hlbg_create(const hlbg_geometry *geom, const hlbg_params *params,
                 const hlbg_iolet *inlets, int32_t n_inlets, const hlbg_iolet *outlets,
                 int32_t n_outlets, hlbg_ctx **out);
+/* Replace the iolets' parameters (BoundaryValues' iolets,
+ * Code/lb/iolets/BoundaryValues.h:21,83): same counts as at creation (the
+ * geometry's iolet ids refer to them), models matching the streamers; the next
+ * step uses the new densities / velocities, positions and normals. */
+int hlbg_set_iolets(hlbg_ctx *ctx, const hlbg_iolet *inlets, int32_t n_inlets,
+                    const hlbg_iolet *outlets, int32_t n_outlets);
 void hlbg_destroy(hlbg_ctx *ctx);
 const char *hlbg_last_error(const hlbg_ctx *ctx);
 

@@ -416,3 +416,38 @@ def test_iolet_flux_balances_at_steady_state():
     phi_in, phi_out = s.IoletFlux()
     assert phi_in > 0 and phi_out < 0
     assert abs(phi_in + phi_out) <= 1e-4 * phi_in
+
+
+def test_set_iolets_is_creating_with_them():
+    """hlbg_set_iolets: new iolet parameters on a context give the same run, bit for
+    bit, as a context created with them, also when changed between steps (against a
+    context created with the new ones and given the state at the change); the
+    counts cannot change and the models must match the streamers."""
+    from hemelb_gb300.lbm import InOutLetCosine
+    old = small_bifurcation(seed=6)
+    new = small_bifurcation(seed=6, peak=0.03, period=150.0)
+    new_out = [InOutLetCosine(tuple(o.position), tuple(o.normal), density_mean=0.9995) for o in new.outlets]
+    a = old.solver()
+    a.SetIolets(new.inlets, new_out)
+    a.SetInitialConditions()
+    a.DoTimeStep(60)
+    b = LBM(new.geometry, new.params, new.inlets, new_out)
+    b.SetInitialConditions()
+    b.DoTimeStep(60)
+    assert np.array_equal(a.GetFOld(), b.GetFOld())
+    # a change between steps: the state at the change, continued with the new iolets
+    c = old.solver()
+    c.SetInitialConditions()
+    c.DoTimeStep(30)
+    d = LBM(new.geometry, new.params, new.inlets, new_out)
+    d.PutF(c.GetFOld(), 0)
+    d.PutF(c.GetFNew(), 1)
+    d.SetTimeStep(31)
+    c.SetIolets(new.inlets, new_out)
+    c.DoTimeStep(30)
+    d.DoTimeStep(30)
+    assert np.array_equal(c.GetFOld(), d.GetFOld())
+    with pytest.raises(capi.HlbgError):
+        c.SetIolets(new.inlets, new_out[:-1])
+    with pytest.raises(capi.HlbgError):
+        c.SetIolets(new_out[:1], new_out)  # pressure iolet on the Ladd inlet streamer
