@@ -133,6 +133,7 @@ class Solver {
  public:
   Solver(const hlbg_geometry& g, const hlbg_params& p, const std::vector<hlbg_iolet>& inlets,
          const std::vector<hlbg_iolet>& outlets) {
+    n_iolets_ = inlets.size() + outlets.size();
     int rc = hlbg_create(&g, &p, inlets.data(), (int32_t)inlets.size(), outlets.data(),
                          (int32_t)outlets.size(), &ctx_);
     if (rc != HLBG_OK) {
@@ -171,9 +172,69 @@ class Solver {
     if (rc != HLBG_OK && rc != HLBG_ERR_UNSTABLE) check(rc, ctx_, "hlbg_reduce");
     return st;
   }
+  /// n steps with the StabilityTester fused in; the stats of the step before the last.
+  hlbg_stats StepMonitored(int n = 1) {
+    hlbg_stats st{};
+    int rc = hlbg_step_monitored(ctx_, n, &st);
+    if (rc != HLBG_OK && rc != HLBG_ERR_UNSTABLE) check(rc, ctx_, "hlbg_step_monitored");
+    return st;
+  }
+  struct Steady {
+    int64_t steps_to_steady, steps_run;
+    double final_rel_du;
+    int status;  // HLBG_OK, HLBG_ERR_TIMEOUT or HLBG_ERR_UNSTABLE
+  };
+  Steady RunToSteady(double tol, double u_ref, int64_t max_steps, int32_t check_batch = 25) {
+    Steady r{};
+    r.status = hlbg_run_to_steady(ctx_, tol, u_ref, max_steps, check_batch, &r.steps_to_steady, &r.steps_run,
+                                  &r.final_rel_du);
+    if (r.status != HLBG_OK && r.status != HLBG_ERR_TIMEOUT && r.status != HLBG_ERR_UNSTABLE)
+      check(r.status, ctx_, "hlbg_run_to_steady");
+    return r;
+  }
+  void SetTimeStep(uint64_t t1) { check(hlbg_set_time_step(ctx_, t1), ctx_, "hlbg_set_time_step"); }
+  void SetIolets(const std::vector<hlbg_iolet>& inlets, const std::vector<hlbg_iolet>& outlets) {
+    check(hlbg_set_iolets(ctx_, inlets.data(), (int32_t)inlets.size(), outlets.data(), (int32_t)outlets.size()),
+          ctx_, "hlbg_set_iolets");
+  }
+  void GetMacro(double* rho, double* u) { check(hlbg_get_macro(ctx_, rho, u), ctx_, "hlbg_get_macro"); }
+  std::vector<double> IoletFlux() {
+    std::vector<double> out(n_iolets_);
+    check(hlbg_iolet_flux(ctx_, out.data(), (int32_t)out.size()), ctx_, "hlbg_iolet_flux");
+    return out;
+  }
+  std::vector<double> WallShearStress() {
+    std::vector<double> out((size_t)SiteCount());
+    check(hlbg_wall_shear_stress(ctx_, out.data()), ctx_, "hlbg_wall_shear_stress");
+    return out;
+  }
+  hlbg_incomp Incompressibility() {
+    hlbg_incomp r{};
+    check(hlbg_incompressibility(ctx_, &r), ctx_, "hlbg_incompressibility");
+    return r;
+  }
+  void WriteCheckpoint(const std::string& path, uint64_t timestep, double voxel_size = 1.0,
+                       const double* origin = nullptr, bool append = false) {
+    const double zero[3] = {0.0, 0.0, 0.0};
+    check(hlbg_write_checkpoint(ctx_, path.c_str(), timestep, voxel_size, origin ? origin : zero, append ? 1 : 0),
+          ctx_, "hlbg_write_checkpoint");
+  }
+  /// Loads the record of `timestep` (the last one when negative); returns its timestep.
+  uint64_t ReadCheckpoint(const std::string& path, int64_t timestep = -1) {
+    uint64_t found = 0;
+    check(hlbg_read_checkpoint(ctx_, path.c_str(), timestep, &found), ctx_, "hlbg_read_checkpoint");
+    return found;
+  }
+  int32_t Autotune(int32_t steps_per_trial = 3) {
+    int32_t v = 0;
+    float ms = 0.f;
+    check(hlbg_autotune(ctx_, steps_per_trial, &v, &ms), ctx_, "hlbg_autotune");
+    return v;
+  }
 
  private:
   hlbg_ctx* ctx_ = nullptr;
+  size_t n_iolets_ = 0;
 };
 
 }  // namespace hemelb_gb300

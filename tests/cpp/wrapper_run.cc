@@ -1,16 +1,21 @@
 // Runs the LB update through the C++ wrapper (hemelb_gb300.hpp) on a site list
 // read from a file, and writes fOld in contiguous site order.
-//   wrapper_run <sites.bin> <steps> <out.bin>
+//   wrapper_run <sites.bin> <steps> <out.bin> [<checkpoint.xtr> <more steps> <restart.bin>]
+// With a checkpoint path, the state after <steps> is also written as an XTR
+// checkpoint, read into a second solver, and both run <more steps>; restart.bin
+// then holds [the continued fOld | the restarted fOld | the restarted solver's
+// iolet fluxes].
 // sites.bin: int64 n, then per site: int64 x,y,z; uint32 wall, iolet; int32 ioid;
 // int32 type; float cut[18]; then int32 n_in, n_out and hlbg_iolet records;
 // then hlbg_params.
 #include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "hemelb_gb300.hpp"
 
 int main(int argc, char** argv) {
-  if (argc != 4) return 2;
+  if (argc != 4 && argc != 7) return 2;
   FILE* f = fopen(argv[1], "rb");
   if (!f) return 3;
   int64_t n = 0;
@@ -45,6 +50,24 @@ int main(int argc, char** argv) {
     FILE* o = fopen(argv[3], "wb");
     fwrite(fo.data(), 8, fo.size(), o);
     fclose(o);
+    if (argc == 7) {
+      const int steps = atoi(argv[2]), more = atoi(argv[5]);
+      s.WriteCheckpoint(argv[4], (uint64_t)steps);
+      hemelb_gb300::Solver r(gb.View(), p, in, out);
+      if (r.ReadCheckpoint(argv[4]) != (uint64_t)steps) return 10;
+      r.SetTimeStep((uint64_t)steps + 1);
+      s.Step(more);
+      r.Step(more);
+      std::vector<double> a(fo.size()), b(fo.size());
+      s.GetF(a.data(), 0);
+      r.GetF(b.data(), 0);
+      const std::vector<double> flux = r.IoletFlux();
+      FILE* q = fopen(argv[6], "wb");
+      fwrite(a.data(), 8, a.size(), q);
+      fwrite(b.data(), 8, b.size(), q);
+      fwrite(flux.data(), 8, flux.size(), q);
+      fclose(q);
+    }
   } catch (const hemelb_gb300::Error& e) {
     fprintf(stderr, "%s\n", e.what());
     return 9;

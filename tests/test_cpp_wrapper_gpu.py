@@ -1,5 +1,6 @@
 """The C++ host wrapper (include/hemelb_gb300.hpp: GeometryBuilder + Solver) drives
-the CUDA update through the C ABI; its result equals the oracle's bit for bit."""
+the CUDA update through the C ABI; its result equals the oracle's bit for bit, and
+an XTR checkpoint written and read through it restarts the run bit for bit."""
 import os
 import struct
 import subprocess
@@ -43,9 +44,18 @@ def test_cpp_wrapper_matches_oracle(tmp_path):
             fh.write(bytes(io))
         fh.write(bytes(p.to_c()))
     out = tmp_path / "f.bin"
-    r = subprocess.run([str(exe), str(sites), "40", str(out)], capture_output=True, text=True)
+    restart = tmp_path / "restart.bin"
+    r = subprocess.run([str(exe), str(sites), "40", str(out), str(tmp_path / "state.xtr"), "15", str(restart)],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     f = np.fromfile(out, dtype=np.float64).reshape(n, 19)
     o.set_equilibrium()
     o.step(40)
     assert np.array_equal(f, o.fold())
+    # the checkpoint restart continues bit for bit, and the fluxes come back
+    rr = np.fromfile(restart, dtype=np.float64)
+    cont, rest, flux = rr[:n * 19], rr[n * 19:2 * n * 19], rr[2 * n * 19:]
+    o.step(15)
+    assert np.array_equal(cont.reshape(n, 19), o.fold())
+    assert np.array_equal(rest, cont)
+    assert flux.shape == (len(inl) + len(outl),) and np.all(np.isfinite(flux))
