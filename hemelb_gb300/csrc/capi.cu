@@ -38,11 +38,13 @@ const int HCY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -
 const int HCZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
 const int HINV[19] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
 
-// Fluid list order within a block: its sites in slot order (HLBG_LIST_SPLIT=0), or
+// Fluid list order within a block: its sites in slot order (HLBG_LIST_SPLIT=0);
 // its bulk sites first and then its boundary sites (1), which keeps most warps on
-// the bulk push path but leaves gaps in each warp's slots.  Measured on the
-// vascular forest: split +4% to +9% for FP16 storage (instruction-bound), -7% for
-// FP32 deviations (bandwidth-bound); the default (-1) splits for FP16 only.
+// the bulk push path but leaves gaps in each warp's slots; or whole 8-site rows,
+// those without a boundary site first (2).  Measured on the vascular forest: 1 is
+// +4% to +9% for FP16 storage (instruction-bound) and -7% for FP32 deviations
+// (bandwidth-bound); 2 is +/-0 for FP32 and +8% for FP16.  The default (-1) is 1
+// for FP16 and 0 otherwise.
 #ifndef HLBG_LIST_SPLIT
 #define HLBG_LIST_SPLIT -1
 #endif
@@ -682,15 +684,28 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
       }
       tmp.clear();
     };
-    const bool split = HLBG_LIST_SPLIT < 0 ? ctx->prec == HLBG_FP16 : HLBG_LIST_SPLIT != 0;
+    const int split = HLBG_LIST_SPLIT < 0 ? (ctx->prec == HLBG_FP16 ? 1 : 0) : HLBG_LIST_SPLIT;
     for (int64_t b = 0; b < nb; ++b) {
-      if (split) {
+      if (split == 1) {
         // bulk sites first, then the boundary sites, so that most warps take the
         // bulk push path and only the warps holding boundary sites the mixed one
         for (int j = 0; j < 512; ++j)
           if (code[b * 512 + j] == 1) tmp.push_back((uint16_t)j);
         for (int j = 0; j < 512; ++j)
           if (code[b * 512 + j] >= 2) tmp.push_back((uint16_t)(j | kListBoundary));
+      } else if (split == 2) {
+        // whole 8-site rows (32-byte sectors in FP32): rows without a boundary site
+        // first, then the others, so warps stay sector-aligned
+        for (int pass = 0; pass < 2; ++pass)
+          for (int row = 0; row < 64; ++row) {
+            bool bnd = false;
+            for (int t = 0; t < 8; ++t) bnd |= code[b * 512 + row * 8 + t] >= 2;
+            if (bnd != (pass == 1)) continue;
+            for (int t = 0; t < 8; ++t) {
+              const uint32_t c = code[b * 512 + row * 8 + t];
+              if (c) tmp.push_back((uint16_t)((row * 8 + t) | (c >= 2 ? kListBoundary : 0u)));
+            }
+          }
       } else {
         for (int j = 0; j < 512; ++j)
           if (code[b * 512 + j]) tmp.push_back((uint16_t)(j | (code[b * 512 + j] >= 2 ? kListBoundary : 0u)));
