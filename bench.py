@@ -45,7 +45,7 @@ B_ALG = {0: 304, 1: 152, 2: 76}  # algorithmic bytes per fluid-site update (2 * 
 # the update kernel each launch shape runs (hlbg_set_launch_variant)
 KERNEL_OF_VARIANT = {-1: "k_stream_collide<P, 128, 2>", 0: "k_stream_collide<P, 128, 10>",
                      1: "k_stream_collide<P, 128, 8>", 2: "k_stream_collide<P, 256, 4>",
-                     3: "k_stream_collide<P, 512, 2>", 4: "k_stream_collide_listed_persist<P, 128, 8>",
+                     3: "k_stream_collide<P, 512, 2>", 4: "k_stream_collide_block<P, 256, 4>",
                      5: "k_stream_collide_listed<P, 128, 9>", 6: "k_stream_collide_listed<P, 128, 8>",
                      7: "k_stream_collide_listed<P, 64, 16>"}
 DTYPE = {0: "f64", 1: "f32", 2: "f16-storage/f32"}

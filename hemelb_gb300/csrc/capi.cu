@@ -140,6 +140,11 @@ struct hlbg_ctx {
   int32_t* d_warp_block = nullptr;  // fluid-list launch (StepArgs::warp_block)
   uint16_t* d_lane_slot = nullptr;
   int64_t n_warps = 0;
+  uint64_t* d_blk_fluid = nullptr;  // block-staged launch (StepArgs::blk_*)
+  uint64_t* d_blk_bnd = nullptr;
+  uint32_t* d_blk_run_off = nullptr;
+  uint16_t* d_blk_runs = nullptr;
+  int32_t* d_stage_err = nullptr;
   std::vector<int32_t> h_flux_slot, h_flux_gi;  // sites with iolet links, their iolet
   int32_t* d_flux_slot = nullptr;
   int32_t* d_flux_gi = nullptr;
@@ -257,6 +262,12 @@ void fill_args(hlbg_ctx* ctx, StepArgs& a) {
   a.slot2site = ctx->d_slot2site;
   a.site2slot = ctx->d_site2slot;
   a.warp_block = ctx->d_warp_block;
+  a.blk_fluid = ctx->d_blk_fluid;
+  a.blk_bnd = ctx->d_blk_bnd;
+  a.blk_run_off = ctx->d_blk_run_off;
+  a.blk_runs = ctx->d_blk_runs;
+  a.n_blocks = ctx->nb;
+  a.stage_err = ctx->d_stage_err;
   a.lane_slot = ctx->d_lane_slot;
   a.n_warps = ctx->n_warps;
   a.site_code = ctx->d_site_code;
@@ -724,6 +735,39 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     if ((rc = upload(ctx, &ctx->d_warp_block, wb))) return rc;
     if ((rc = upload(ctx, &ctx->d_lane_slot, ls))) return rc;
   }
+  if (!HLBG_PACK && !HLBG_BLOCK_ORDER) {
+    // block-staged launch: fluid / boundary bitmaps per block (slot order) and the
+    // runs of consecutive rows that hold fluid
+    std::vector<uint64_t> bf((size_t)nb * 8, 0), bb((size_t)nb * 8, 0);
+    std::vector<uint32_t> roff((size_t)nb + 1, 0);
+    std::vector<uint16_t> runs;
+    for (int64_t b = 0; b < nb; ++b) {
+      roff[b] = (uint32_t)runs.size();
+      for (int j = 0; j < 512; ++j) {
+        const uint32_t c = code[b * 512 + j];
+        if (c) bf[b * 8 + (j >> 6)] |= 1ull << (j & 63);
+        if (c >= 2) bb[b * 8 + (j >> 6)] |= 1ull << (j & 63);
+      }
+      int row = 0;
+      while (row < 64) {
+        if (((bf[b * 8 + (row >> 3)] >> ((row & 7) * 8)) & 0xffull) == 0) {
+          ++row;
+          continue;
+        }
+        int end = row + 1;
+        while (end < 64 && ((bf[b * 8 + (end >> 3)] >> ((end & 7) * 8)) & 0xffull) != 0) ++end;
+        runs.push_back((uint16_t)(row | ((end - row) << 6)));
+        row = end;
+      }
+    }
+    roff[nb] = (uint32_t)runs.size();
+    if ((rc = upload(ctx, &ctx->d_blk_fluid, bf))) return rc;
+    if ((rc = upload(ctx, &ctx->d_blk_bnd, bb))) return rc;
+    if ((rc = upload(ctx, &ctx->d_blk_run_off, roff))) return rc;
+    if ((rc = upload(ctx, &ctx->d_blk_runs, runs))) return rc;
+  }
+  if ((rc = dev_alloc(ctx, &ctx->d_stage_err, 1))) return rc;
+  CK(cudaMemset(ctx->d_stage_err, 0, sizeof(int32_t)));
   if ((rc = upload(ctx, &ctx->d_block_nbr, bnbr))) return rc;
   if (HLBG_PACK) {  // the kernels read the tables only in packed builds
     if ((rc = upload(ctx, &ctx->d_slot2site, slot2site))) return rc;
@@ -957,6 +1001,14 @@ std::vector<IoletDev> iolet_table(const hlbg_ctx* ctx) {
   return iod;
 }
 
+// A block-staged CTA that gave up waiting for its staged rows leaves a flag.
+int check_stage_err(hlbg_ctx* ctx) {
+  int32_t e = 0;
+  CK(cudaMemcpy(&e, ctx->d_stage_err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (e) return fail(ctx, HLBG_ERR_TIMEOUT, "a block-staged update gave up waiting for its copies");
+  return HLBG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -994,6 +1046,7 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_steady_n,  ctx->d_slot2site, ctx->d_site2slot, ctx->d_mon_u,
                   ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result,
                   ctx->d_warp_block, ctx->d_lane_slot, ctx->d_b_normal, ctx->d_wss,
+                  ctx->d_blk_fluid, ctx->d_blk_bnd, ctx->d_blk_run_off, ctx->d_blk_runs, ctx->d_stage_err,
                   ctx->d_flux_slot, ctx->d_flux_gi, ctx->d_flux};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1695,7 +1748,7 @@ int hlbg_set_launch_variant(hlbg_ctx* ctx, int32_t variant) {
 int hlbg_sync(hlbg_ctx* ctx) {
   if (!ctx) return HLBG_ERR_INVAL;
   CK(cudaStreamSynchronize(ctx->stream));
-  return HLBG_OK;
+  return check_stage_err(ctx);
 }
 
 int hlbg_stream_and_collide_range(hlbg_ctx* ctx, int64_t first, int64_t count) {
@@ -2052,7 +2105,7 @@ int hlbg_time_kernels(hlbg_ctx* ctx, int32_t nsteps, float* collide_ms, float* p
   if (e != cudaSuccess) return fail(ctx, HLBG_ERR_CUDA, cudaGetErrorString(e));
   *collide_ms = c;
   *post_ms = p;
-  return HLBG_OK;
+  return check_stage_err(ctx);
 }
 
 int hlbg_time_steps(hlbg_ctx* ctx, int32_t nsteps, float* ms) {
@@ -2068,7 +2121,7 @@ int hlbg_time_steps(hlbg_ctx* ctx, int32_t nsteps, float* ms) {
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   CK(cudaEventSynchronize(ctx->ev1));
   CK(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
-  return HLBG_OK;
+  return check_stage_err(ctx);
 }
 
 }  // extern "C"

@@ -150,6 +150,16 @@ struct StepArgs {
   const int32_t* warp_block;
   const uint16_t* lane_slot;
   int64_t n_warps;
+  // Block-staged launch: per block its fluid and boundary-site bitmaps (8 words,
+  // bit j = slot j), and its runs of consecutive 8-slot rows that hold fluid
+  // (blk_runs[blk_run_off[b] .. blk_run_off[b+1]), start row | length << 6);
+  // stage_err is set when a CTA's wait for its staged rows gives up.
+  const uint64_t* blk_fluid;
+  const uint64_t* blk_bnd;
+  const uint32_t* blk_run_off;
+  const uint16_t* blk_runs;
+  int64_t n_blocks;
+  int32_t* stage_err;
   const uint32_t* site_code;
   const uint8_t* block_bulk;  // 1: all 512 slots are bulk sites
   const uint32_t* b_wall;

@@ -586,6 +586,38 @@ __device__ __forceinline__ void collide_slot(const StepArgs& a, int64_t s,
 
 // One warp of the fluid list: 32 fluid sites of one block (or the zero-fill of its
 // solid slots that share sectors with fluid), so no lane is spent on a solid slot.
+// Collide one lane's site (code 0: an idle lane, computed on the rest state and
+// stored nowhere) and push its post-collision values, on the warp's bulk path when
+// no lane has a boundary record.  tabreg: the block's neighbour table in lanes
+// 0..26.  Every lane of the warp must take part (shuffles, ballot).
+template <int P, bool MON>
+__device__ __forceinline__ void collide_and_push(const StepArgs& a, int64_t b, int j, int64_t s, int l,
+                                                 uint32_t code, int32_t tabreg, typename Calc<P>::T* f,
+                                                 const int32_t* __restrict__ block_xyz, MonAccT<P>& acc,
+                                                 bool check, const MonOld<P>& uo) {
+  using S = typename Store<P>::S;
+  using T = typename Calc<P>::T;
+  S* fn = static_cast<S*>(a.f_new);
+  T fpost[Q];
+  T m0, mx, my, mz;
+  collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
+  if constexpr (MON) {
+    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check, uo);
+  }
+  const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
+  const bool bnd = code >= 2;
+  if (__ballot_sync(0xffffffffu, bnd) == 0) {
+    PushBulk<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, code == 1, fpost);
+  } else {
+    const int64_t r = bnd ? (int64_t)code - 2 : 0;
+    const uint64_t links = bnd ? a.b_links[r] : 0ull;
+    const int type = bnd ? (int)a.b_type[r] : 0;
+    const int ioid = bnd ? a.b_ioid[r] : 0;
+    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, j, b * (Q * kSites), code != 0, false, links,
+                         r, type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
+  }
+}
+
 // The unit's list entries (block e, this lane's slot js) are loaded by the caller.
 template <int P, bool MON>
 __device__ __forceinline__ void collide_listed_unit(const StepArgs& a, int32_t e, unsigned js,
@@ -617,7 +649,7 @@ __device__ __forceinline__ void collide_listed_unit(const StepArgs& a, int32_t e
   const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + j;
   MonOld<P> uo;
   if constexpr (MON) uo.load(a, s, check && on);
-  T f[Q], fpost[Q];
+  T f[Q];
   if (on) {
 #pragma unroll
     for (int i = 0; i < Q; ++i) f[i] = St::load(fo, i * kSites, a);
@@ -625,23 +657,7 @@ __device__ __forceinline__ void collide_listed_unit(const StepArgs& a, int32_t e
 #pragma unroll
     for (int i = 0; i < Q; ++i) f[i] = (T)(P == 0 ? weight_d(i) : 0.0);
   }
-  T m0, mx, my, mz;
-  collide_any<P>(a, b, f, m0, mx, my, mz, fpost);
-  if constexpr (MON) {
-    if (code != 0) mon_site<P>(a, s, f, m0, mx, my, mz, acc, check, uo);
-  }
-  const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
-  const bool bnd = code >= 2;
-  if (__ballot_sync(0xffffffffu, bnd) == 0) {
-    PushBulk<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, code == 1, fpost);
-  } else {
-    const int64_t r = bnd ? (int64_t)code - 2 : 0;
-    const uint64_t links = bnd ? a.b_links[r] : 0ull;
-    const int type = bnd ? (int)a.b_type[r] : 0;
-    const int ioid = bnd ? a.b_ioid[r] : 0;
-    PushMixed<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, j, b * (Q * kSites), code != 0, false, links,
-                         r, type, ioid, fpost, m0, mx, my, mz, b, block_xyz);
-  }
+  collide_and_push<P, MON>(a, b, j, s, l, code, tabreg, f, block_xyz, acc, check, uo);
 }
 
 template <int P, bool MON>
@@ -662,43 +678,156 @@ __global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed(StepArg
   if constexpr (MON) mon_write_partial<P>(a, acc);
 }
 
-// Persistent fluid list: a grid of resident CTAs whose warps stride over the list
-// (warp k takes units k, k + G, k + 2G, ... with G warps in the grid, so the grid
-// still sweeps the list in order), each loading its next unit's entries before it
-// works on the current one, so the index latency overlaps the update.
+// ---------------------------------------------------------------------------
+// Block-staged launch (FP32 / FP16 storage): one CTA per 8^3 block.  Its rows of
+// the old distributions that hold fluid (whole 8-slot rows, every direction) come
+// into shared memory by bulk asynchronous copies (cp.async.bulk, completion counted
+// on an mbarrier), so a CTA has its whole block in flight at once and no lane waits
+// on a list entry; the CTA then collides its fluid sites from shared memory in
+// compacted warps (the k-th thread takes the k-th fluid site of the block), pushes
+// as the other launches do, and zero-fills the solid slots of its fluid rows.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Position of the n-th (from 0) set bit of w (n < popc(w)), by halving.
+__device__ __forceinline__ int select32(uint32_t w, int n) {
+  int pos = 0, c;
+  c = __popc(w & 0xffffu);
+  if (n >= c) { n -= c; pos += 16; w >>= 16; }
+  c = __popc(w & 0xffu);
+  if (n >= c) { n -= c; pos += 8; w >>= 8; }
+  c = __popc(w & 0xfu);
+  if (n >= c) { n -= c; pos += 4; w >>= 4; }
+  c = __popc(w & 0x3u);
+  if (n >= c) { n -= c; pos += 2; w >>= 2; }
+  if (n >= (int)(w & 1u)) pos += 1;
+  return pos;
+}
+
+// Wait for phase `parity` of the mbarrier at shared address bar; false after
+// kStageWaitLimit polls (each try_wait may suspend the thread for a while).
+constexpr int64_t kStageWaitLimit = 1ll << 24;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int64_t it = 0; it < kStageWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 template <int P, int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB)
-    k_stream_collide_listed_persist(StepArgs a, const int32_t* block_xyz) {
-  MonAccT<P> acc = mon_neutral_t<P>();  // unused: persistent steps are not monitored
-  const int lane = threadIdx.x & 31;
-  const int64_t G = (int64_t)gridDim.x * (THREADS / 32);
-  int64_t w = ((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5;
-  if (w >= a.n_warps) return;
-  int32_t e = __ldg(a.warp_block + w);
-  unsigned js = __ldg(a.lane_slot + w * 32 + lane);
-  for (; w < a.n_warps; w += G) {
-    const int64_t wn = w + G;
-    int32_t en = 0;
-    unsigned jsn = 0xffffu;
-    if (wn < a.n_warps) {
-      en = __ldg(a.warp_block + wn);
-      jsn = __ldg(a.lane_slot + wn * 32 + lane);
+__global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_block(StepArgs a, const int32_t* block_xyz) {
+  static_assert(P != 0, "the staged block holds FP32 or FP16 values");
+  using S = typename Store<P>::S;
+  using T = typename Calc<P>::T;
+  extern __shared__ __align__(128) unsigned char stage_raw[];
+  S* stage = reinterpret_cast<S*>(stage_raw);  // [Q][kSites]
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t wfl[16], wbd[16], wpre[17];
+  __shared__ uint32_t stage_bytes;
+  const int64_t b = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const uint32_t bar = smem_u32(&mbar);
+  const uint32_t r0 = __ldg(a.blk_run_off + b), r1 = __ldg(a.blk_run_off + b + 1);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    uint32_t bytes = 0;
+    for (uint32_t r = r0; r < r1; ++r) bytes += (uint32_t)(__ldg(a.blk_runs + r) >> 6) * 8u * (uint32_t)sizeof(S);
+    stage_bytes = bytes * Q;
+  }
+  if (tid < 16) {
+    wfl[tid] = __ldg(reinterpret_cast<const uint32_t*>(a.blk_fluid + b * 8) + tid);
+    wbd[tid] = __ldg(reinterpret_cast<const uint32_t*>(a.blk_bnd + b * 8) + tid);
+  }
+  __syncthreads();
+  if (tid == 0)
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(stage_bytes)
+                 : "memory");
+  __syncthreads();
+  // the copies: (run, direction) pairs over the threads; sizes and both addresses
+  // are multiples of 16 bytes (rows of 8 values of 2 or 4 bytes)
+  const uint32_t ncopy = (r1 - r0) * Q;
+  const char* src0 = static_cast<const char*>(a.f_old) + (size_t)b * (Q * kSites) * sizeof(S);
+  const uint32_t dst0 = smem_u32(stage);
+  for (uint32_t k = tid; k < ncopy; k += THREADS) {
+    const uint32_t run = __ldg(a.blk_runs + r0 + k / Q), d = k % Q;
+    const uint32_t off = (d * kSites + (run & 63u) * 8u) * (uint32_t)sizeof(S);
+    const uint32_t size = (run >> 6) * 8u * (uint32_t)sizeof(S);
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst0 + off),
+        "l"(src0 + off), "r"(size), "r"(bar)
+        : "memory");
+  }
+  const int32_t tabreg = lane < 27 ? __ldg(a.block_nbr + b * 27 + lane) : 0;
+  if (tid == 0) {
+    uint32_t acc = 0;
+    for (int k = 0; k < 16; ++k) {
+      wpre[k] = acc;
+      acc += __popc(wfl[k]);
     }
-    collide_listed_unit<P, false>(a, e, js, block_xyz, acc, false);
-    e = en;
-    js = jsn;
+    wpre[16] = acc;
+  }
+  const bool landed = mbar_wait(bar, 0);
+  if (!__syncthreads_and(landed)) {  // every copy this CTA issued has to land before it may exit
+    if (tid == 0) atomicExch(a.stage_err, 1);
+    mbar_wait(bar, 0);
+    return;
+  }
+  const int nf = (int)wpre[16];
+  MonAccT<P> acc = mon_neutral_t<P>();  // unused: staged steps are not monitored
+  const MonOld<P> uo;
+  for (int base = tid & ~31; base < nf; base += THREADS) {  // warp-uniform trips
+    const int t = base + lane;
+    const bool on = t < nf;
+    int j = 0;
+    if (on) {
+      int k = 0;  // the word holding the t-th fluid slot
+#pragma unroll
+      for (int h = 8; h > 0; h >>= 1)
+        if ((int)wpre[k + h] <= t) k += h;
+      j = k * 32 + select32(wfl[k], t - (int)wpre[k]);
+    }
+    const int64_t s = b * kSites + j;
+    const bool bnd = on && ((wbd[j >> 5] >> (j & 31)) & 1u);
+    const uint32_t code = on ? (bnd ? a.site_code[s] : 1u) : 0u;
+    T f[Q];
+#pragma unroll
+    for (int d = 0; d < Q; ++d) {
+      if constexpr (P == 1)
+        f[d] = on ? stage[d * kSites + j] : 0.f;
+      else
+        f[d] = on ? __half2float(stage[d * kSites + j]) * a.fp16_inv_scale : 0.f;
+    }
+    collide_and_push<P, false>(a, b, j, s, j, code, tabreg, f, block_xyz, acc, false, uo);
+  }
+  // solid slots of the rows that hold fluid: zeros complete their sectors
+  S* fn = static_cast<S*>(a.f_new);
+  for (int j = tid; j < kSites; j += THREADS) {
+    const uint32_t w = wfl[j >> 5];
+    if (((w >> (j & 24)) & 0xffu) != 0 && !((w >> (j & 31)) & 1u)) {
+#pragma unroll
+      for (int d = 0; d < Q; ++d) Store<P>::store(fn, fidx(b * kSites + j, d), (T)0, a);
+    }
   }
 }
 
 template <int P, int THREADS, int MINB>
-void launch_listed_persist(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // MINB CTAs per SM are resident by the launch bounds (no shared memory)
-  const int64_t need = (a.n_warps * 32 + THREADS - 1) / THREADS;
-  const int64_t g = std::min<int64_t>(need, (int64_t)sms * MINB);
-  if (g > 0) k_stream_collide_listed_persist<P, THREADS, MINB><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
+void launch_block_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
+  constexpr size_t smem = (size_t)Q * kSites * sizeof(typename Store<P>::S);
+  static bool carveout = false;  // as much shared memory as the SM has, once
+  if (!carveout) {
+    cudaFuncSetAttribute(k_stream_collide_block<P, THREADS, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         100);
+    carveout = true;
+  }
+  if (a.n_blocks > 0)
+    k_stream_collide_block<P, THREADS, MINB><<<(unsigned)a.n_blocks, THREADS, smem, st>>>(a, bxyz);
 }
 
 template <int P, int THREADS, int MINB, bool MON>
@@ -1254,8 +1383,13 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     if (a.mon_u && variant == 0) variant = 1;                                                   \
     if (a.mon_u && variant >= 4) variant = 6;                                                   \
     if (variant == 4) {                                                                         \
-      launch_listed_persist<P, 128, (P == 0 ? 2 : 8)>(a, bxyz, st);                             \
-      return;                                                                                   \
+      if constexpr (P != 0) {                                                                   \
+        if (a.blk_runs) {                                                                       \
+          launch_block_staged<P, 256, 4>(a, bxyz, st);                                          \
+          return;                                                                               \
+        }                                                                                       \
+      }                                                                                         \
+      variant = 6; /* FP64, or a layout without the block tables */                             \
     }                                                                                           \
     if (variant == 5) {                                                                         \
       launch_listed<P, 128, (P == 0 ? 2 : 9), false>(a, bxyz, st);                              \

@@ -301,10 +301,11 @@ int hlbg_incompressibility(hlbg_ctx *ctx, hlbg_incomp *out);
  * the iolets and dominates the time to steady state. */
 int hlbg_average_time_levels(hlbg_ctx *ctx);
 /* Select the stream-and-collide launch shape by index (0..7: all slots at 128x10,
- * 128x8, 256x4, 512x2 threads x resident CTAs; the fluid list, whose warps hold
- * only fluid slots, as a persistent 128x8 grid that loads each warp's next entries
- * ahead, and at 128x9, 128x8 and 64x16); FP64 runs two CTAs per SM.  Monitored
- * steps run every fluid-list index as 128x8.  No reference counterpart. */
+ * 128x8, 256x4, 512x2 threads x resident CTAs; one CTA per block with the block's
+ * fluid rows staged in shared memory by bulk asynchronous copies (FP32 / FP16;
+ * FP64 runs index 6 instead); the fluid list, whose warps hold only fluid slots,
+ * at 128x9, 128x8 and 64x16); FP64 runs two CTAs per SM.  Monitored steps run
+ * every index from 4 up as the 128x8 fluid list.  No reference counterpart. */
 int hlbg_set_launch_variant(hlbg_ctx *ctx, int32_t variant);
 /* Autotuner: time each launch shape / schedule of the stream-and-collide kernel
  * (threads per CTA x resident CTAs per SM, per-slot grid or persistent grid) on
