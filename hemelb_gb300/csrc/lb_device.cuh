@@ -424,4 +424,19 @@ __device__ __forceinline__ double ladd_correction64(const IoletDev& io, double u
   return 2. * weight_d(d) * dd / (1.0 / 3.0);
 }
 
+// The same correction in FP32 for the FP32 / FP16 forms (their link arithmetic is
+// FP32 throughout; only the iolet bookkeeping and the reductions stay FP64).
+__device__ __forceinline__ float ladd_correction32(const IoletDev& io, float umax, float rho, int l_x, int l_y,
+                                                   int l_z, int d) {
+  const float n0 = (float)io.n[0], n1 = (float)io.n[1], n2 = (float)io.n[2];
+  const float dx = ((float)l_x + 0.5f * (float)c_cx[d]) - (float)io.pos[0];
+  const float dy = ((float)l_y + 0.5f * (float)c_cy[d]) - (float)io.pos[1];
+  const float dz = ((float)l_z + 0.5f * (float)c_cz[d]) - (float)io.pos[2];
+  const float z = dx * n0 + dy * n1 + dz * n2;
+  const float rSq = (dx * dx + dy * dy + dz * dz - z * z) / (float)(io.radius * io.radius);
+  const float s = umax * (1.f - rSq) * rho;
+  const float dd = (n0 * (float)c_cx[d] + n1 * (float)c_cy[d] + n2 * (float)c_cz[d]) * s;
+  return 6.f * weight_f(d) * dd;  // 2 w (c . u rho) / c_s^2
+}
+
 }  // namespace hlbg

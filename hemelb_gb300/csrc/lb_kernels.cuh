@@ -59,12 +59,15 @@ __device__ __noinline__ typename Calc<P>::T iolet_link_value(
       const float gzv = (float)io.nf[2] * comp * grho_f;
       const float inv_g = 1.f / grho_f;
       const float mde = c_cx[un] * gxv + c_cy[un] * gyv + c_cz[un] * gzv;
-      return (float)weight_d(un) *
+      return weight_f(un) *
              ((gdr - 1.5f * (gxv * gxv + gyv * gyv + gzv * gzv) * inv_g) + mde * (3.f + 4.5f * inv_g * mde));
     }
   }
-  const double rho = (P == 0) ? (double)m0 : 1.0 + (double)m0;
-  return fpost_d - (T)ladd_correction64(io, a.iolet_umax[gi], rho, gx, gy, gz, d);
+  if constexpr (P == 0) {
+    return fpost_d - ladd_correction64(io, a.iolet_umax[gi], m0, gx, gy, gz, d);
+  } else {
+    return fpost_d - ladd_correction32(io, (float)a.iolet_umax[gi], 1.f + m0, gx, gy, gz, d);
+  }
 }
 
 // Entry k of the 27-block table around a site's block (neighbour block index,
