@@ -21,7 +21,7 @@ max |du| / U_ref <= 1e-6.  Training samples are solved with a one-off average of
 the first two time levels (``hlbg_average_time_levels``), which removes the
 lattice's slowly decaying staggered-momentum mode and shortens data generation
 about sixfold; held-out samples are solved exactly as the reference would, from
-rest, and that plain solve judges the error of every warm-started run.
+rest, and that plain solve is the yardstick for the error of every warm-started run.
 
 U_ref, the StabilityTester reference speed, is the Poiseuille centreline speed
 of the inlet tube under the mean pressure gradient: (drho c_s^2 / box) R_in^2 / (4 nu).
@@ -470,7 +470,7 @@ def rel_l2(a, b):
 
 def evaluate(net: UNet, samples, box: int, plain_warm: int = 0, log=None):
     """Held-out evaluation.  Per sample, on one context: the plain solve from rest
-    (the reference's start; its field judges the others), rest with the one-off
+    (the reference's start; the others are measured against its field), rest with the one-off
     averaging, and the warm start (prediction, averaging); for the first
     `plain_warm` samples also the warm start without averaging.  Wall times include
     the prediction and the field upload."""
