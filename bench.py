@@ -320,8 +320,11 @@ def main():
     per_launch = kms / args.steps
     peak, peak_kind = measured_peak()
     achieved = B_ALG[prec] * n / (per_launch / 1e3) / 1e9
-    kname = KERNEL_OF_VARIANT.get(variant if prec != 0 else (5 if variant >= 5 else -1),
-                                  "k_stream_collide").replace("<P", "<%d" % prec)
+    if prec == 0:  # FP64 runs two CTAs per SM in every shape, the fluid list from index 4 up
+        kname = ("k_stream_collide_listed<0, %d, 2>" % (64 if variant == 7 else 128)) if variant >= 4 \
+            else "k_stream_collide<0, 128, 2>"
+    else:
+        kname = KERNEL_OF_VARIANT.get(variant, "k_stream_collide").replace("<P", "<%d" % prec)
     base = kname.split("<")[0]
     # DRAM bytes per site: a one-pass capture of this workload, else a small-case full capture
     tps = profile_traffic("%s_%s_%s_dram" % (base, args.precision, args.workload)) \
