@@ -1481,6 +1481,7 @@ int hlbg_write_checkpoint(hlbg_ctx* ctx, const char* path, uint64_t timestep, do
   // One timestep record: the step number, then per site in contiguous order its
   // grid position and its 19 distributions of the current state (the reference's
   // GetFOld), as LocalPropertyOutput::Write does for a "distributions" field.
+  // The record is encoded and written in chunks of sites.
   if (!ctx || !path) return HLBG_ERR_INVAL;
   const std::string opath = offset_path(path);
   if (opath.empty()) return fail(ctx, HLBG_ERR_INVAL, "checkpoint path needs an extension");
@@ -1491,15 +1492,9 @@ int hlbg_write_checkpoint(hlbg_ctx* ctx, const char* path, uint64_t timestep, do
   if (!rc) rc = hlbg_site_coords(ctx, xyz.data());
   if (rc) return rc;
   const std::vector<uint8_t> head = checkpoint_header((uint64_t)n, voxel_size, origin);
-  XdrOut rec;
-  rec.b.reserve(8 + (size_t)n * (12 + 19 * 8));
-  rec.u64(timestep);
-  for (int64_t i = 0; i < n; ++i) {
-    for (int c = 0; c < 3; ++c) rec.u32((uint32_t)xyz[3 * i + c]);
-    for (int d = 0; d < 19; ++d) rec.f64(f[(size_t)i * 19 + d]);
-  }
-  FILE* fp = append ? std::fopen(path, "rb") : nullptr;
-  if (fp) {  // append to a file of the same geometry
+  const uint64_t rec_len = 8 + (uint64_t)n * (12 + 19 * 8);
+  FILE* fp = nullptr;
+  if (append && (fp = std::fopen(path, "rb"))) {  // append to a file of the same geometry
     std::vector<uint8_t> old(head.size());
     const bool same = std::fread(old.data(), 1, old.size(), fp) == old.size() &&
                       std::memcmp(old.data() + 48, head.data() + 48, head.size() - 48) == 0;
@@ -1507,26 +1502,40 @@ int hlbg_write_checkpoint(hlbg_ctx* ctx, const char* path, uint64_t timestep, do
     if (!same) return fail(ctx, HLBG_ERR_INVAL, "checkpoint file holds another geometry");
     fp = std::fopen(path, "ab");
     if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot open checkpoint file");
-    const bool ok = std::fwrite(rec.b.data(), 1, rec.b.size(), fp) == rec.b.size();
-    std::fclose(fp);
-    return ok ? HLBG_OK : fail(ctx, HLBG_ERR_INVAL, "checkpoint write failed");
+  } else {
+    append = 0;
+    fp = std::fopen(path, "wb");
+    if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot create checkpoint file");
   }
-  fp = std::fopen(path, "wb");
-  if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot create checkpoint file");
-  bool ok = std::fwrite(head.data(), 1, head.size(), fp) == head.size() &&
-            std::fwrite(rec.b.data(), 1, rec.b.size(), fp) == rec.b.size();
-  std::fclose(fp);
-  // offset file: one rank, its chunk of the first timestep (LocalPropertyOutput::WriteOffsetFile)
-  XdrOut off;
-  off.u32(kHemeLbMagic);
-  off.u32(kOffMagic);
-  off.u32(kOffVersion);
-  off.u32(1);  // int32 rank count
-  off.u64(head.size());
-  off.u64(head.size() + rec.b.size());
-  FILE* fo = std::fopen(opath.c_str(), "wb");
-  ok = ok && fo && std::fwrite(off.b.data(), 1, off.b.size(), fo) == off.b.size();
-  if (fo) std::fclose(fo);
+  bool ok = append || std::fwrite(head.data(), 1, head.size(), fp) == head.size();
+  XdrOut rec;
+  rec.u64(timestep);
+  constexpr int64_t kChunk = 1 << 16;  // sites per write
+  for (int64_t i0 = 0; ok && i0 < n; i0 += kChunk) {
+    const int64_t i1 = std::min(n, i0 + kChunk);
+    rec.b.reserve(rec.b.size() + (size_t)(i1 - i0) * (12 + 19 * 8));
+    for (int64_t i = i0; i < i1; ++i) {
+      for (int c = 0; c < 3; ++c) rec.u32((uint32_t)xyz[3 * i + c]);
+      for (int d = 0; d < 19; ++d) rec.f64(f[(size_t)i * 19 + d]);
+    }
+    ok = std::fwrite(rec.b.data(), 1, rec.b.size(), fp) == rec.b.size();
+    rec.b.clear();
+  }
+  if (n == 0 && ok) ok = std::fwrite(rec.b.data(), 1, rec.b.size(), fp) == rec.b.size();
+  ok = (std::fclose(fp) == 0) && ok;
+  if (ok && !append) {
+    // offset file: one rank, its chunk of the first timestep (LocalPropertyOutput::WriteOffsetFile)
+    XdrOut off;
+    off.u32(kHemeLbMagic);
+    off.u32(kOffMagic);
+    off.u32(kOffVersion);
+    off.u32(1);  // int32 rank count
+    off.u64(head.size());
+    off.u64(head.size() + rec_len);
+    FILE* fo = std::fopen(opath.c_str(), "wb");
+    ok = fo && std::fwrite(off.b.data(), 1, off.b.size(), fo) == off.b.size();
+    if (fo) ok = (std::fclose(fo) == 0) && ok;
+  }
   return ok ? HLBG_OK : fail(ctx, HLBG_ERR_INVAL, "checkpoint write failed");
 }
 
@@ -1534,21 +1543,21 @@ int hlbg_read_checkpoint(hlbg_ctx* ctx, const char* path, int64_t timestep, uint
   // LocalDistributionInput::LoadDistribution (Code/extraction/LocalDistributionInput.cc:
   // 56-251): the header checks, the record of the requested timestep (the last one
   // if timestep < 0), each site's grid position against this geometry's contiguous
-  // order, and the distributions into both time levels.
+  // order, and the distributions into both time levels.  Only the header, the
+  // records' timesteps and the chosen record are read.
   if (!ctx || !path) return HLBG_ERR_INVAL;
   FILE* fp = std::fopen(path, "rb");
   if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot open checkpoint file");
-  std::vector<uint8_t> buf;
-  {
-    std::fseek(fp, 0, SEEK_END);
-    const long sz = std::ftell(fp);
-    std::fseek(fp, 0, SEEK_SET);
-    buf.resize(sz > 0 ? (size_t)sz : 0);
-    const size_t got = std::fread(buf.data(), 1, buf.size(), fp);
-    std::fclose(fp);
-    if (got != buf.size()) return fail(ctx, HLBG_ERR_INVAL, "checkpoint read failed");
-  }
-  XdrIn in{buf.data(), buf.size()};
+  struct Closer {
+    FILE* f;
+    ~Closer() { std::fclose(f); }
+  } closer{fp};
+  std::fseek(fp, 0, SEEK_END);
+  const long long fsize = (long long)std::ftell(fp);
+  std::fseek(fp, 0, SEEK_SET);
+  std::vector<uint8_t> hb((size_t)std::min<long long>(std::max<long long>(fsize, 0), 4096));
+  if (std::fread(hb.data(), 1, hb.size(), fp) != hb.size()) return fail(ctx, HLBG_ERR_INVAL, "checkpoint read failed");
+  XdrIn in{hb.data(), hb.size()};
   if (in.u32() != kHemeLbMagic || in.u32() != kXtrMagic) return fail(ctx, HLBG_ERR_INVAL, "not an extraction file");
   if (in.u32() != kXtrVersion) return fail(ctx, HLBG_ERR_INVAL, "extraction version is not 5");
   for (int k = 0; k < 4; ++k) in.f64();  // voxel size, origin
@@ -1561,19 +1570,22 @@ int hlbg_read_checkpoint(hlbg_ctx* ctx, const char* path, int64_t timestep, uint
       in.at - field_start != fhl)
     return fail(ctx, HLBG_ERR_INVAL, "not a D3Q19 distribution checkpoint");
   if ((int64_t)nsites != ctx->nsites) return fail(ctx, HLBG_ERR_INVAL, "checkpoint site count differs");
-  const size_t head = in.at, rec = 8 + (size_t)nsites * (12 + 19 * 8);
-  if ((buf.size() - head) % rec || buf.size() == head)
+  const long long head = (long long)in.at, rec = 8 + (long long)nsites * (12 + 19 * 8);
+  if (fsize <= head || (fsize - head) % rec)
     return fail(ctx, HLBG_ERR_INVAL, "checkpoint length is not a whole number of timesteps");
-  const size_t nt = (buf.size() - head) / rec;
-  auto ts_at = [&](size_t k) {
-    XdrIn t{buf.data() + head + k * rec, 8};
+  const long long nt = (fsize - head) / rec;
+  bool io_ok = true;
+  auto ts_at = [&](long long k) {
+    uint8_t b8[8];
+    if (std::fseek(fp, (long)(head + k * rec), SEEK_SET) != 0 || std::fread(b8, 1, 8, fp) != 8) io_ok = false;
+    XdrIn t{b8, 8};
     return t.u64();
   };
-  size_t k = nt - 1;
+  long long k = nt - 1;
   if (timestep >= 0) {  // the timesteps are increasing: binary search
-    size_t lo = 0, len = nt;
+    long long lo = 0, len = nt;
     while (len) {
-      const size_t half = len / 2, m = lo + half;
+      const long long half = len / 2, m = lo + half;
       if (ts_at(m) < (uint64_t)timestep) {
         lo = m + 1;
         len -= half + 1;
@@ -1582,22 +1594,29 @@ int hlbg_read_checkpoint(hlbg_ctx* ctx, const char* path, int64_t timestep, uint
       }
     }
     if (lo >= nt || ts_at(lo) != (uint64_t)timestep)
-      return fail(ctx, HLBG_ERR_INVAL, "timestep not found in checkpoint file");
+      return fail(ctx, HLBG_ERR_INVAL, io_ok ? "timestep not found in checkpoint file" : "checkpoint read failed");
     k = lo;
   }
+  const uint64_t ts = ts_at(k);
+  if (!io_ok) return fail(ctx, HLBG_ERR_INVAL, "checkpoint read failed");
   std::vector<int32_t> xyz((size_t)nsites * 3);
   int rc = hlbg_site_coords(ctx, xyz.data());
   if (rc) return rc;
-  XdrIn d{buf.data() + head + k * rec, rec};
-  const uint64_t ts = d.u64();
   std::vector<double> f((size_t)nsites * 19);
-  for (uint64_t i = 0; i < nsites; ++i) {
-    for (int c = 0; c < 3; ++c)
-      if ((int32_t)d.u32() != xyz[3 * i + c])
-        return fail(ctx, HLBG_ERR_INVAL, "site " + std::to_string(i) + " of the checkpoint is not this geometry's");
-    for (int q = 0; q < 19; ++q) f[i * 19 + q] = d.f64();
+  constexpr uint64_t kChunk = 1 << 16;  // sites per read
+  std::vector<uint8_t> buf;
+  for (uint64_t i0 = 0; i0 < nsites; i0 += kChunk) {  // the file position follows the timestep
+    const uint64_t i1 = std::min<uint64_t>(nsites, i0 + kChunk);
+    buf.resize((size_t)(i1 - i0) * (12 + 19 * 8));
+    if (std::fread(buf.data(), 1, buf.size(), fp) != buf.size()) return fail(ctx, HLBG_ERR_INVAL, "truncated checkpoint");
+    XdrIn d{buf.data(), buf.size()};
+    for (uint64_t i = i0; i < i1; ++i) {
+      for (int c = 0; c < 3; ++c)
+        if ((int32_t)d.u32() != xyz[3 * i + c])
+          return fail(ctx, HLBG_ERR_INVAL, "site " + std::to_string(i) + " of the checkpoint is not this geometry's");
+      for (int q = 0; q < 19; ++q) f[i * 19 + q] = d.f64();
+    }
   }
-  if (!d.ok) return fail(ctx, HLBG_ERR_INVAL, "truncated checkpoint");
   if ((rc = hlbg_put_f(ctx, f.data(), 0)) || (rc = hlbg_put_f(ctx, f.data(), 1))) return rc;
   if (found) *found = ts;
   return HLBG_OK;

@@ -80,3 +80,20 @@ def test_checkpoint_reader_rejects_other_files(tmp_path):
     open(good, "wb").write(X.checkpoint_header(len(coords)) + X.checkpoint_record(7, coords, g))
     assert s.ReadCheckpoint(good) == 7
     assert np.array_equal(s.GetFOld(), g)
+
+
+def test_checkpoint_of_a_geometry_larger_than_one_write_chunk(tmp_path):
+    """A pipe of ~125k sites: the record is encoded, written and read back in
+    several chunks of sites; the bytes equal the oracle's and the state returns."""
+    c = cases.pipe(radius=20.0, length=100)
+    s = c.solver()
+    s.SetInitialConditions()
+    s.DoTimeStep(5)
+    assert s.n_sites > 65536  # two chunks or more
+    path = str(tmp_path / "big.xtr")
+    s.WriteCheckpoint(path, 5)
+    coords, f = s.site_coords(), s.GetFOld()
+    assert open(path, "rb").read() == X.checkpoint_header(len(coords)) + X.checkpoint_record(5, coords, f)
+    r = c.solver()
+    assert r.ReadCheckpoint(path) == 5
+    assert np.array_equal(r.GetFOld(), f)
