@@ -143,11 +143,12 @@ void hlbo_feq(const hlbo_params *p, double density, const double mom[3], double 
 }
 
 /* HydroVars + Kernel: LBGK (Code/lb/kernels/LBGK.h:29-63) or TRT
- * (Code/lb/kernels/TRT.h:160-188).  TRT's own moments call does not compile in
- * this reference revision (TRT.h:130-138 names a 9-argument
- * CalculateDensityMomentumFEq that Lattice.h does not declare); the kernel is
- * restated with LBGK's moments (Lattice.h:471-483), TRT's f_neq = f - f_eq and
- * its pair relaxation over the nine (i, iBar) opposite pairs with i < iBar. */
+ * (Code/lb/kernels/TRT.h:94-122, magic parameter 3/16).  TRT's moments are
+ * LBGK's (Lattice.h:471-483, the overload TRT.h:62-92 means to call), f_neq =
+ * f - f_eq, the rest direction relaxed with omega+ (TRT.h:108-112) and the nine
+ * opposite pairs (i, iBar) with i < iBar relaxed with omega+/omega- in the
+ * order of TRT.h:115-121.  Pinned bit for bit to the reference's TRT.h compiled
+ * with the build-time patch of oracle/refbuild/build_ref.py. */
 static void collide(const lat_t *L, const hlbo_params *p, const double *f, double *rho,
                     double m[3], double u[3], double *feq, double *fpost) {
   const int q = L->q;

@@ -1,6 +1,7 @@
 """Regenerate the golden vectors with the reference's own LB code compiled from
-its sources (oracle/refbuild, scalar evaluation order).  Run in a checkout that
-has the reference tree:  python tests/golden/make_golden.py"""
+its sources (oracle/refbuild, scalar evaluation order; TRT from the reference's
+TRT.h with the recipe's build-time patch).  Run in a checkout that has the
+reference tree:  python tests/golden/make_golden.py [name ...]"""
 import os
 import sys
 
@@ -20,7 +21,7 @@ def main():
     build_lib()
     build_oracle()
     out_dir = os.path.dirname(os.path.abspath(__file__))
-    for name in golden_cases.NAMES:
+    for name in (sys.argv[1:] or golden_cases.NAMES):
         g, inl, outl, p, steps, f0 = golden_cases.build(name)
         o = OracleLBM(g.view, p, inl, outl, order=ORDER_SCALAR)
         o.set_equilibrium()

@@ -7,9 +7,9 @@ import subprocess
 import pytest
 
 from hemelb_gb300 import capi
+from oracle.refbuild.build_ref import REF
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("HEMELB_REFERENCE", "/root/reference") + "/Code"
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")

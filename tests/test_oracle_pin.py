@@ -4,7 +4,9 @@
    (oracle/refbuild): bit-exact in both of the reference's evaluation orders
    (scalar = aarch64 build, SSE3 = x86_64 build) on geometries that exercise
    every collision type, SBB and BFL walls (with PostStep), Nash and Ladd iolets,
-   D3Q19 and D3Q15.  Skipped where the reference sources are absent.
+   D3Q19 and D3Q15, LBGK and TRT (the reference's Code/lb/kernels/TRT.h with the
+   recipe's build-time patch of its two compile defects).  Skipped where the
+   reference sources are absent.
 2. Against golden vectors the compiled reference produced (tests/golden/*.npz,
    made by tests/golden/make_golden.py), which travel with the repository.
 """
@@ -95,6 +97,40 @@ def test_four_cube_d3q15_anisotropic_matches_reference(wall):
     g, inl, outl = four_cube(15)
     p = LbmParameters(tau=0.8, wall=wall)
     f0 = anisotropic(64, 15)
+    for variant, order in _variants():
+        _compare_with_reference(g.view, p, inl, outl, 3, variant, order, f0=f0)
+
+
+@needs_ref
+def test_trt_pipe_matches_reference():
+    """TRT, magic parameter 3/16 (Code/lb/kernels/TRT.h:94-122), SBB walls, Nash
+    iolets: the benchmark's physics on a small pipe."""
+    c = cases.pipe(radius=6.0, length=30)
+    c.params.kernel = capi.KERNEL_TRT
+    for variant, order in _variants():
+        _compare_with_reference(c.geometry.view, c.params, c.inlets, c.outlets, 60, variant, order)
+
+
+@needs_ref
+@pytest.mark.parametrize("tau", [0.51, 0.6, 1.0, 1.9])
+def test_trt_bifurcation_bfl_ladd_matches_reference(tau):
+    """TRT over all six collision types with BFL walls and a Ladd inlet, at τ near
+    the stability limit, at τ = 1 (ω+ = −1) and far above it (τ− < τ+ and > τ+)."""
+    g, inl, outl, p = golden_cases.bifurcation_bfl_ladd()
+    p.kernel = capi.KERNEL_TRT
+    p.tau = tau
+    for variant, order in _variants():
+        _compare_with_reference(g.view, p, inl, outl, 40, variant, order)
+
+
+@needs_ref
+@pytest.mark.parametrize("q", [15, 19])
+def test_trt_four_cube_anisotropic_matches_reference(q):
+    """TRT on the reference's streamer-test fixture with anisotropic f, where f_neq
+    differs in every direction so a mis-paired (i, iBar) would show."""
+    g, inl, outl = four_cube(q)
+    p = LbmParameters(tau=0.7, kernel=capi.KERNEL_TRT, wall=capi.WALL_BFL)
+    f0 = anisotropic(64, q)
     for variant, order in _variants():
         _compare_with_reference(g.view, p, inl, outl, 3, variant, order, f0=f0)
 
