@@ -67,6 +67,12 @@ def parse():
                     help="launch shape of the update (hlbg_set_launch_variant); -1: autotune")
     ap.add_argument("--precision", default="fp32dev", choices=["fp64", "fp32dev", "fp16"])
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--check-interval", type=int, default=6,
+                    help="StabilityTester check interval of the e2e path (hlbg_set_monitor_interval): "
+                         "the reference checks once per phased-broadcast round trip, 2 x tree depth "
+                         "steps, i.e. 6 on a 1000-rank run (spread factor 10)")
+    ap.add_argument("--ref-seconds", type=float, default=10.0,
+                    help="target length of the reference arm's timed region")
     ap.add_argument("--cpu-sites", type=int, default=2_000_000,
                     help="fluid sites in the CPU sample (Morton-contiguous blocks)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -247,16 +253,25 @@ def cpu_sample(case, n_sites: int, seconds: float, threads: int):
 def run_reference_arm(args):
     threads = os.cpu_count() or 1
     case, prec, cfg = make_case(args)
+    cfg["storage"] = "fp64"  # the reference's own distributions are doubles
     from oracle.oracle import ORDER_SCALAR, OracleLBM  # noqa: F401
     n, _, _, o = cpu_sample(case, args.cpu_sites, 0.0, threads)
     for _ in range(args.warmup):
         o.step(1, threads)
+    # each bench step is m LB time steps over the sample, m chosen so that the
+    # timed region lasts about --ref-seconds
     t0 = time.perf_counter()
-    o.step(args.steps, threads)
+    o.step(1, threads)
+    one = time.perf_counter() - t0
+    m = max(1, int(args.ref_seconds / max(one * args.steps, 1e-9)))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(m, threads)
     dt = time.perf_counter() - t0
-    mlups = n * args.steps / dt / 1e6
-    sample = ("%d fluid sites (the first Morton-ordered blocks of the workload), FP64, scalar "
-              "(aarch64) evaluation order, OpenMP over %d threads" % (n, threads))
+    mlups = n * m * args.steps / dt / 1e6
+    sample = ("%d fluid sites (the first Morton-ordered blocks of the workload), %d LB steps per bench "
+              "step, FP64, scalar (aarch64) evaluation order, OpenMP over %d threads" % (n, m, threads))
+    cfg["lb_steps_per_bench_step"] = m
     line = {"impl": "reference", "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -335,26 +350,36 @@ def main():
                 "algorithmic_bytes_per_launch": B_ALG[prec] * n,
                 "kernel": "hlbg::" + kname, "launch_ms": per_launch}
     # ---- end to end through the C ABI: per step, H2D of that step's iolet values,
-    # the update with the StabilityTester fused into it, and the D2H read-back of
-    # its stats (stability, mass, max |du| for the convergence test), synchronous
+    # the update with the StabilityTester fused into it on its check cadence, and the
+    # D2H read-back of the stats (stability, mass, max |du| for the convergence
+    # test), synchronous
     st = capi.Stats()
     ke = max(1, min(args.e2e_steps, args.steps))
-    capi.check(lbm._lib.hlbg_step_monitored(lbm.ctx, 1, C.byref(st)), lbm.ctx)  # records velocities
-    barrier(dist)
-    lbm._lib.hlbg_sync(lbm.ctx)
-    t0 = time.perf_counter()
-    for _ in range(ke):
-        rc = lbm._lib.hlbg_step_monitored(lbm.ctx, 1, C.byref(st))
-        if rc not in (0, capi.HLBG_ERR_UNSTABLE):
-            capi.check(rc, lbm.ctx)
-    dt = time.perf_counter() - t0
-    barrier(dist)
-    dt = max_over_ranks(dist, dt)
+
+    def e2e_rate(interval):
+        capi.check(lbm._lib.hlbg_set_monitor_interval(lbm.ctx, interval), lbm.ctx)
+        for _ in range(interval + 1):  # one full check cycle before the clock starts
+            capi.check(lbm._lib.hlbg_step_monitored(lbm.ctx, 1, C.byref(st)), lbm.ctx)
+        barrier(dist)
+        lbm._lib.hlbg_sync(lbm.ctx)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            rc = lbm._lib.hlbg_step_monitored(lbm.ctx, 1, C.byref(st))
+            if rc not in (0, capi.HLBG_ERR_UNSTABLE):
+                capi.check(rc, lbm.ctx)
+        dt = time.perf_counter() - t0
+        barrier(dist)
+        return WORLD * n * ke / max_over_ranks(dist, dt) / 1e6
+
+    every = e2e_rate(1)
+    cadence = e2e_rate(args.check_interval)
     n_io = len(case.inlets) + len(case.outlets)
-    e2e = {"value": WORLD * n * ke / dt / 1e6, "unit": "MLUPS", "steps": ke,
+    e2e = {"value": cadence, "unit": "MLUPS", "steps": ke,
            "h2d_bytes_per_step": 2 * 8 * n_io, "d2h_bytes_per_step": 5 * 8,
+           "check_interval": args.check_interval, "value_check_every_step": every,
            "path": "hlbg_step_monitored(1) per step: iolet values in, update with the fused "
-                   "StabilityTester, its stats (mass, max |du|, min f, unstable count) out"}
+                   "StabilityTester checking every %d steps, its stats (mass, max |du|, min f, "
+                   "unstable count) out" % args.check_interval}
     stable = st.unstable_sites == 0 and st.time_step > 0
     # ---- CPU baseline ---------------------------------------------------------
     cpu = None

@@ -29,7 +29,7 @@ UNITS = [
     ("capi.cu", ["--fmad=false"]),
     ("nn_kernels.cu", []),
 ]
-HOST_UNITS = ["synthgeo.cpp"]
+HOST_UNITS = ["synthgeo.cpp", "halo.cpp"]
 
 
 def _run(cmd):

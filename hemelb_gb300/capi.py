@@ -111,6 +111,7 @@ SIGNATURES = {
     "hlbg_average_time_levels": (C.c_int, [C.c_void_p]),
     "hlbg_set_launch_variant": (C.c_int, [C.c_void_p, C.c_int32]),
     "hlbg_step_monitored": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Stats)]),
+    "hlbg_set_monitor_interval": (C.c_int, [C.c_void_p, C.c_int32]),
     "hlbg_incompressibility": (C.c_int, [C.c_void_p, C.POINTER(Incomp)]),
     "hlbg_wall_shear_stress": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hlbg_iolet_flux": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
@@ -135,6 +136,26 @@ SIGNATURES = {
     "hlbg_time_steps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
     "hlbg_time_kernels": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "hlbg_version": (C.c_char_p, []),
+    # multi-rank halo: host-side index maps (no device work)
+    "hlbg_halo_partition": (C.c_int, [C.POINTER(Geometry), C.c_int32, C.POINTER(C.c_int32)]),
+    "hlbg_halo_create": (C.c_int, [C.POINTER(Geometry), C.POINTER(C.c_int32), C.c_int32, C.c_int32,
+                                   C.POINTER(C.c_void_p)]),
+    "hlbg_halo_destroy": (None, [C.c_void_p]),
+    "hlbg_halo_last_error": (C.c_char_p, [C.c_void_p]),
+    "hlbg_halo_local_geometry": (C.c_int, [C.c_void_p, C.POINTER(Geometry), C.POINTER(C.c_int64)]),
+    "hlbg_halo_block_source": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "hlbg_halo_edge_blocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint8)]),
+    "hlbg_halo_peer_count": (C.c_int32, [C.c_void_p]),
+    "hlbg_halo_peer": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int64)]),
+    "hlbg_halo_offsets": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int8), C.POINTER(C.c_int16),
+                                    C.c_int64, C.POINTER(C.c_int64)]),
+    "hlbg_halo_pack_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "hlbg_halo_unpack_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "hlbg_halo_check": (C.c_int, [C.c_void_p]),
+    "hlbg_storage_bytes": (C.c_int, [C.c_void_p]),
+    "hlbg_halo_list": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int8),
+                                 C.POINTER(C.c_int16)]),
     # include/hemelb_gb300_nn.h: the surrogate's kernels (device pointers, stream last)
     "hlbg_nn_conv3d": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,

@@ -15,7 +15,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <map>
 #include <new>
 #include <string>
@@ -133,6 +132,7 @@ struct hlbg_ctx {
   double min_density = 1.0;
   uint64_t t1 = 1;
   int cur = 0;
+  double* noalloc_scratch = nullptr;  // device address of hlbg_reduce_noalloc's static array
   void* f[2] = {nullptr, nullptr};
   int32_t* d_block_nbr = nullptr;
   int32_t* d_block_xyz = nullptr;
@@ -163,6 +163,8 @@ struct hlbg_ctx {
   double* d_wss = nullptr;          // wall shear stress output, allocated on first use
   int32_t* d_rec_slot = nullptr;  // slot of each record
   std::vector<int32_t> h_new_of_old;  // device block index of each input block
+  std::vector<uint16_t> h_site2slot;  // in-block slot of each local site (built by hlbg_halo_offsets)
+  int32_t* d_halo_err = nullptr;      // out-of-range offsets seen by the halo pack / unpack
   double* d_blk_omega = nullptr;      // optional per-block (omega+, omega-)
   // CUDA graphs of k steps, keyed by (k, parity of the current array)
   struct GraphKey {
@@ -209,6 +211,8 @@ struct hlbg_ctx {
   double* d_mon_result = nullptr;
   double* h_mon_result = nullptr;  // pinned
   bool mon_recorded = false;       // host view: velocities of the current state recorded
+  int32_t mon_interval = 1;        // hlbg_step_monitored checks the steps t with t % interval == 0
+  int64_t mon_checked_t = -1;      // the step of the last check hlbg_step_monitored launched
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t dev_bytes = 0;
@@ -823,6 +827,7 @@ int mon_prepare(hlbg_ctx* ctx) {
   if ((rc = dev_alloc(ctx, &ctx->d_mon_part2, kMonFields * (size_t)kMonStage2))) return rc;
   if ((rc = dev_alloc(ctx, &ctx->d_mon_state, 1))) return rc;
   if ((rc = dev_alloc(ctx, &ctx->d_mon_result, kMonResult))) return rc;
+  CK(cudaMemsetAsync(ctx->d_mon_result, 0, kMonResult * sizeof(double), ctx->stream));  // no check yet
   CK(cudaMallocHost((void**)&ctx->h_mon_result, kMonResult * sizeof(double)));
   CK(cudaMemsetAsync(ctx->d_mon_state, 0, sizeof(int32_t), ctx->stream));
   ctx->mon_recorded = false;
@@ -948,6 +953,7 @@ int graph_steps(hlbg_ctx* ctx, int n, bool check) {
   CK(cudaGraphLaunch(it->second, ctx->stream));
   if (ctx->n_io) CK(cudaEventRecord(ctx->io_copied, ctx->stream));
   ctx->cur ^= (n & 1);
+  if (check) ctx->mon_checked_t = (int64_t)(ctx->t1 + n - 1);
   ctx->t1 += n;
   if (check) ctx->mon_recorded = true;
   return HLBG_OK;
@@ -1011,6 +1017,10 @@ int check_stage_err(hlbg_ctx* ctx) {
 
 }  // namespace
 
+namespace {
+int prepare_noalloc(hlbg_ctx* ctx);  // defined beside hlbg_reduce_noalloc
+}  // namespace
+
 extern "C" {
 
 int hlbg_set_iolets(hlbg_ctx* ctx, const hlbg_iolet* inlets, int32_t n_inlets, const hlbg_iolet* outlets,
@@ -1047,7 +1057,7 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result,
                   ctx->d_warp_block, ctx->d_lane_slot, ctx->d_b_normal, ctx->d_wss,
                   ctx->d_blk_fluid, ctx->d_blk_bnd, ctx->d_blk_run_off, ctx->d_blk_runs, ctx->d_stage_err,
-                  ctx->d_flux_slot, ctx->d_flux_gi, ctx->d_flux};
+                  ctx->d_flux_slot, ctx->d_flux_gi, ctx->d_flux, ctx->d_halo_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
@@ -1093,6 +1103,7 @@ int hlbg_create(const hlbg_geometry* g, const hlbg_params* p, const hlbg_iolet* 
   CK(cudaEventCreate(&ctx->ev1));
   CK(cudaEventCreateWithFlags(&ctx->io_copied, cudaEventDisableTiming));
   CK(cudaEventRecord(ctx->io_copied, ctx->stream));
+  if ((rc = prepare_noalloc(ctx))) return rc;
   if ((rc = build_layout(ctx, g))) return rc;
   // iolet constants
   ctx->n_io = (int)(ctx->inlets.size() + ctx->outlets.size());
@@ -1346,29 +1357,50 @@ int hlbg_run_to_steady(hlbg_ctx* ctx, double tol, double u_ref, int64_t max_step
   return HLBG_OK;
 }
 
+int hlbg_set_monitor_interval(hlbg_ctx* ctx, int32_t interval) {
+  if (!ctx || interval < 1) return HLBG_ERR_INVAL;
+  ctx->mon_interval = interval;
+  return HLBG_OK;
+}
+
 int hlbg_step_monitored(hlbg_ctx* ctx, int32_t nsteps, hlbg_stats* out) {
-  // nsteps time steps with the StabilityTester fused into the update; the stats
-  // are those of the check made during the last step, i.e. of the step before it.
+  // nsteps time steps with the StabilityTester fused into the update.  With the
+  // check interval K (hlbg_set_monitor_interval, default 1), step t checks when
+  // t % K == 0 -- comparing the velocities of the state it collides with those the
+  // step before recorded -- the step before a check records only, and the others
+  // run the plain update.  The stats are those of the last check made.
   if (!ctx || nsteps < 1 || !out) return HLBG_ERR_INVAL;
   if (!ctx->initialised) return fail(ctx, HLBG_ERR_STATE, "no initial condition set");
   int rc = mon_prepare(ctx);
   if (rc) return rc;
   cudaStream_t st = ctx->stream;
+  const uint64_t K = (uint64_t)ctx->mon_interval;
   StepArgs a;
   for (int done = 0; done < nsteps;) {
     const int n = std::min(kStepBatch, nsteps - done);
     if ((rc = upload_iolet_table(ctx, n, st))) return rc;
     for (int k = 0; k < n; ++k) {
+      const uint64_t t = ctx->t1;
+      const bool check = t % K == 0;
+      const bool record = !check && (t + 1) % K == 0;
       fill_args(ctx, a);
       a.iolet_rho = ctx->d_io_tab + (size_t)k * 2 * ctx->n_io;
       a.iolet_umax = a.iolet_rho + ctx->n_io;
-      mon_args(ctx, a);
+      if (check || record) mon_args(ctx, a);
+      // a record-only step compares nothing: the velocities on record are older
+      if (record) CK(cudaMemsetAsync(ctx->d_mon_state, 0, sizeof(int32_t), st));
       if ((rc = launch_collide(ctx, a, st))) return rc;
       if ((rc = run_post(ctx, st, ctx->d_ps_slot, ctx->d_ps_dir, ctx->d_ps_q, ctx->n_ps))) return rc;
       ctx->cur ^= 1;
       ctx->t1++;
-      if ((rc = mon_reduce(ctx, a, false, st))) return rc;
-      ctx->mon_recorded = true;
+      if (check) {
+        if ((rc = mon_reduce(ctx, a, false, st))) return rc;
+        ctx->mon_checked_t = (int64_t)t;
+      } else if (record) {
+        // the next step's check is valid (any nonzero word marks the record present)
+        CK(cudaMemsetAsync(ctx->d_mon_state, 1, sizeof(int32_t), st));
+      }
+      ctx->mon_recorded = check || record;
     }
     done += n;
   }
@@ -1380,7 +1412,7 @@ int hlbg_step_monitored(hlbg_ctx* ctx, int32_t nsteps, hlbg_stats* out) {
   out->max_du = valid ? r[1] : 0.0;
   out->min_f = valid ? r[2] : 0.0;
   out->unstable_sites = valid ? (int64_t)r[3] : 0;
-  out->time_step = valid ? (int64_t)ctx->t1 - 1 : -1;
+  out->time_step = valid ? ctx->mon_checked_t : -1;
   return valid && r[3] > 0.0 ? HLBG_ERR_UNSTABLE : HLBG_OK;
 }
 
@@ -1498,8 +1530,30 @@ int hlbg_write_checkpoint(hlbg_ctx* ctx, const char* path, uint64_t timestep, do
     std::vector<uint8_t> old(head.size());
     const bool same = std::fread(old.data(), 1, old.size(), fp) == old.size() &&
                       std::memcmp(old.data() + 48, head.data() + 48, head.size() - 48) == 0;
+    // hlbg_read_checkpoint finds a timestep by binary search over the records, so
+    // they must stay in increasing timestep order: compare with the last record's.
+    long long fsize = -1;
+    uint64_t last_ts = 0;
+    bool has_last = false, whole = false;
+    if (same && std::fseek(fp, 0, SEEK_END) == 0 && (fsize = (long long)std::ftell(fp)) >= 0) {
+      const long long body = fsize - (long long)head.size();
+      whole = body >= 0 && body % (long long)rec_len == 0;
+      if (whole && body > 0) {
+        uint8_t b8[8];
+        has_last = std::fseek(fp, (long)(fsize - (long long)rec_len), SEEK_SET) == 0 &&
+                   std::fread(b8, 1, 8, fp) == 8;
+        XdrIn t{b8, 8};
+        last_ts = has_last ? t.u64() : 0;
+        whole = has_last;
+      }
+    }
     std::fclose(fp);
     if (!same) return fail(ctx, HLBG_ERR_INVAL, "checkpoint file holds another geometry");
+    if (!whole) return fail(ctx, HLBG_ERR_INVAL, "checkpoint length is not a whole number of timesteps");
+    if (has_last && timestep <= last_ts)
+      return fail(ctx, HLBG_ERR_INVAL,
+                  "checkpoint timestep " + std::to_string(timestep) + " does not follow the file's last, " +
+                      std::to_string(last_ts));
     fp = std::fopen(path, "ab");
     if (!fp) return fail(ctx, HLBG_ERR_INVAL, "cannot open checkpoint file");
   } else {
@@ -1699,7 +1753,7 @@ int hlbg_incompressibility(hlbg_ctx* ctx, hlbg_incomp* out) {
   out->max_velocity = valid ? r[7] : 0.0;
   // IncompressibilityChecker::GetMaxRelativeDensityDifference, REFERENCE_DENSITY = 1
   out->max_relative_density_difference = valid ? r[6] - r[5] : 0.0;
-  out->time_step = valid ? (int64_t)ctx->t1 - 1 : -1;
+  out->time_step = valid ? ctx->mon_checked_t : -1;
   return HLBG_OK;
 }
 
@@ -1998,29 +2052,37 @@ int hlbg_reduce(hlbg_ctx* ctx, hlbg_stats* out) {
 // ---- allocation-free StabilityTester reduction --------------------------------
 // Scratch of hlbg_reduce_noalloc: the per-CTA partials of k_monitor (mass, max|du|,
 // min f, unstable count) for at most kNoAllocParts reduction blocks, laid out as
-// four consecutive runs of kNoAllocParts values.  Every GPU that loads the library
-// holds these 2 MiB until the process exits.  Host code must not use the symbol
-// as a pointer: the device address comes from cudaGetSymbolAddress, once per device.
+// four consecutive runs of kNoAllocParts values (2 MiB).  The array belongs to this
+// translation unit's device module: the module, and with it the array, is placed on
+// a GPU when the module loads there -- at library load with eager module loading,
+// or with lazy loading (CUDA_MODULE_LOADING=LAZY, the default since CUDA 12.2) on
+// the first use of the module on that device.  It then stays until the process
+// exits or the device is reset.  Host code must not use the symbol as a pointer:
+// the device address comes from cudaGetSymbolAddress.
 static constexpr int64_t kNoAllocParts = HLBG_NOALLOC_MAX_SLOTS / 256;
 static __device__ __align__(256) double g_reduce_scratch[4 * kNoAllocParts];
 
 namespace {
-std::mutex g_scratch_mu;
-void* g_scratch_addr[256] = {};
-
-int scratch_address(hlbg_ctx* ctx, double** out) {
-  int dev = -1;
-  CK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 256) return fail(ctx, HLBG_ERR_CUDA, "device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_reduce_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(ctx, HLBG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_scratch_addr[dev] = p;
+// Run by hlbg_create with the context's device current.  Looking up the array's
+// address is this module's first use on the device, so under lazy loading the
+// 2 MiB are placed here, at context creation, not inside a later
+// hlbg_reduce_noalloc call; loading the monitor kernels now keeps their lazy
+// load out of that call as well.  The address is kept per context: a context
+// does not outlive a reset of its device, and a context created after a reset
+// looks the array up again.
+int prepare_noalloc(hlbg_ctx* ctx) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return fail(ctx, HLBG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
   }
-  *out = static_cast<double*>(g_scratch_addr[dev]);
+  ctx->noalloc_scratch = static_cast<double*>(p);
+  e = ctx->prec == 0 ? preload_monitor_0() : (ctx->prec == 1 ? preload_monitor_1() : preload_monitor_2());
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, HLBG_ERR_CUDA, std::string("monitor kernels: ") + cudaGetErrorString(e));
+  }
   return HLBG_OK;
 }
 }  // namespace
@@ -2034,9 +2096,8 @@ int hlbg_reduce_noalloc(hlbg_ctx* ctx, hlbg_stats* out) {
     return fail(ctx, HLBG_ERR_INVAL,
                 "hlbg_reduce_noalloc: " + std::to_string(ctx->nslot) + " slots exceed its limit of " +
                     std::to_string(HLBG_NOALLOC_MAX_SLOTS) + " (use hlbg_reduce)");
-  double* scratch = nullptr;
-  int rc = scratch_address(ctx, &scratch);
-  if (rc) return rc;
+  double* scratch = ctx->noalloc_scratch;
+  if (!scratch) return fail(ctx, HLBG_ERR_INVAL, "hlbg_reduce_noalloc: context has no scratch address");
   // Every partial k_monitor reads is written earlier in the same call (one per
   // CTA, then the final pass into element 0 of each run), so nothing needs clearing.
   MonitorArgs ma{};
@@ -2144,3 +2205,68 @@ int hlbg_time_steps(hlbg_ctx* ctx, int32_t nsteps, float* ms) {
 }
 
 }  // extern "C"
+
+// ---- multi-rank exchange on the device ----------------------------------------
+extern "C" {
+
+int hlbg_halo_offsets(hlbg_ctx* ctx, const int32_t* block, const int8_t* direction, const int16_t* site,
+                      int64_t n, int64_t* out) {
+  if (!ctx || n < 0 || (n && (!block || !direction || !site || !out))) return HLBG_ERR_INVAL;
+  if (ctx->h_site2slot.empty()) {  // invert the in-block order once
+    ctx->h_site2slot.resize(ctx->h_slot2site.size());
+    for (size_t s = 0; s < ctx->h_slot2site.size(); ++s)
+      ctx->h_site2slot[(s & ~(size_t)511) | ctx->h_slot2site[s]] = (uint16_t)(s & 511);
+  }
+  const int64_t nin = (int64_t)ctx->h_new_of_old.size();
+  for (int64_t i = 0; i < n; ++i) {
+    if (block[i] < 0 || block[i] >= nin || direction[i] < 0 || direction[i] >= 19 || site[i] < 0 ||
+        site[i] >= 512)
+      return fail(ctx, HLBG_ERR_INVAL, "halo entry " + std::to_string(i) + " out of range");
+    const int64_t b = ctx->h_new_of_old[block[i]];
+    const int64_t slot = b * 512 + ctx->h_site2slot[(size_t)b * 512 + site[i]];
+    out[i] = fidx(slot, direction[i]);
+  }
+  return HLBG_OK;
+}
+
+static int halo_copy(hlbg_ctx* ctx, const int64_t* offsets, int64_t n, void* buf, int unpack) {
+  if (!ctx || n < 0 || (n && (!offsets || !buf))) return HLBG_ERR_INVAL;
+  if (!ctx->d_halo_err) {
+    int rc = dev_alloc(ctx, &ctx->d_halo_err, 1);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(ctx->d_halo_err, 0, sizeof(int32_t), ctx->stream));
+  }
+  void* fnew = ctx->f[ctx->cur ^ 1];
+  const int64_t limit = (int64_t)19 * ctx->nslot;
+  switch (ctx->prec) {
+    case 0: launch_halo_copy_0(fnew, offsets, n, limit, buf, unpack, ctx->d_halo_err, ctx->stream); break;
+    case 1: launch_halo_copy_1(fnew, offsets, n, limit, buf, unpack, ctx->d_halo_err, ctx->stream); break;
+    default: launch_halo_copy_2(fnew, offsets, n, limit, buf, unpack, ctx->d_halo_err, ctx->stream); break;
+  }
+  CK(cudaGetLastError());
+  return HLBG_OK;
+}
+
+int hlbg_halo_pack_device(hlbg_ctx* ctx, const int64_t* offsets, int64_t n, void* buf) {
+  return halo_copy(ctx, offsets, n, buf, 0);
+}
+
+int hlbg_halo_unpack_device(hlbg_ctx* ctx, const int64_t* offsets, int64_t n, const void* buf) {
+  return halo_copy(ctx, offsets, n, const_cast<void*>(buf), 1);
+}
+
+int hlbg_halo_check(hlbg_ctx* ctx) {
+  if (!ctx) return HLBG_ERR_INVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (!ctx->d_halo_err) return HLBG_OK;
+  int32_t e = 0;
+  CK(cudaMemcpy(&e, ctx->d_halo_err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (!e) return HLBG_OK;
+  CK(cudaMemset(ctx->d_halo_err, 0, sizeof(int32_t)));
+  return fail(ctx, HLBG_ERR_INVAL, "a halo pack or unpack was given an offset outside the distributions");
+}
+
+int hlbg_storage_bytes(const hlbg_ctx* ctx) { return ctx ? (int)ctx->elem : 0; }
+
+}  // extern "C"
+

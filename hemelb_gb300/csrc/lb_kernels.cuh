@@ -1372,6 +1372,40 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
 }
 }  // namespace hlbg
 
+namespace hlbg {
+// Multi-rank exchange: copy stored distributions (the storage element type, so the
+// exchange is exact in every form) between the new-distribution array and a
+// contiguous buffer, at element offsets from hlbg_halo_offsets.  An offset outside
+// [0, limit) is skipped and flagged in *err (a bad list must not write elsewhere).
+template <int P>
+__global__ void k_halo_pack(const void* f, const int64_t* off, int64_t n, int64_t limit, void* buf,
+                            int32_t* err) {
+  using S = typename Store<P>::S;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t o = off[i];
+  if (o < 0 || o >= limit) {
+    atomicOr(err, 1);
+    return;
+  }
+  static_cast<S*>(buf)[i] = static_cast<const S*>(f)[o];
+}
+
+template <int P>
+__global__ void k_halo_unpack(void* f, const int64_t* off, int64_t n, int64_t limit, const void* buf,
+                              int32_t* err) {
+  using S = typename Store<P>::S;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t o = off[i];
+  if (o < 0 || o >= limit) {
+    atomicOr(err, 1);
+    return;
+  }
+  static_cast<S*>(f)[o] = static_cast<const S*>(buf)[i];
+}
+}  // namespace hlbg
+
 #define HLBG_INSTANTIATE(P)                                                                     \
   namespace hlbg {                                                                              \
   void launch_stream_collide_##P(const StepArgs& a, const int32_t* bxyz, cudaStream_t st,      \
@@ -1475,11 +1509,25 @@ void launch_sc(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
     unsigned g = (unsigned)((ga.count + 255) / 256);                                            \
     if (g) k_macro<P><<<g, 256, 0, st>>>(ga);                                                   \
   }                                                                                             \
+  cudaError_t preload_monitor_##P() {                                                           \
+    cudaFuncAttributes fa;                                                                      \
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_monitor<P>);                                   \
+    return e != cudaSuccess ? e : cudaFuncGetAttributes(&fa, k_monitor_final);                  \
+  }                                                                                             \
   void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st) {                   \
     (void)grid;                                                                                 \
     const int64_t nparts = (ma.nslot + 255) / 256;                                              \
     k_monitor<P><<<(unsigned)nparts, 256, 0, st>>>(ma);                                         \
     k_monitor_final<<<1, 256, 0, st>>>(ma, nparts);                                             \
+  }                                                                                             \
+  void launch_halo_copy_##P(void* f, const int64_t* off, int64_t n, int64_t limit, void* buf,     \
+                            int unpack, int32_t* err, cudaStream_t st) {                        \
+    unsigned g = (unsigned)((n + 255) / 256);                                                   \
+    if (!g) return;                                                                             \
+    if (unpack)                                                                                 \
+      k_halo_unpack<P><<<g, 256, 0, st>>>(f, off, n, limit, buf, err);                          \
+    else                                                                                        \
+      k_halo_pack<P><<<g, 256, 0, st>>>(f, off, n, limit, buf, err);                            \
   }                                                                                             \
   void launch_wss_##P(const WssArgs& wa, cudaStream_t st) {                                     \
     unsigned g = (unsigned)((wa.count + 255) / 256);                                            \

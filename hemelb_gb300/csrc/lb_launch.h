@@ -129,11 +129,15 @@ struct FluxArgs {
   void launch_scatter_##P(const GatherArgs& ga, cudaStream_t st);                    \
   void launch_macro_##P(const GatherArgs& ga, cudaStream_t st);                      \
   void launch_monitor_##P(const MonitorArgs& ma, int grid, cudaStream_t st);          \
+  /* load the monitor kernels now (with lazy module loading they load on first use) */ \
+  cudaError_t preload_monitor_##P();                                                 \
   int64_t monitored_grid_##P(int64_t nslot, int variant, int64_t n_warps);                                   \
   void launch_mon_reduce_##P(const double* part, int64_t nparts, double* part2, int64_t n2,    \
                              int32_t* mon_state, double* result, const SteadyArgs& sa,        \
                              int steady, cudaStream_t st);                                     \
   void launch_average_##P(const AverageArgs& aa, cudaStream_t st);                    \
+  void launch_halo_copy_##P(void* f, const int64_t* off, int64_t n, int64_t limit, void* buf, \
+                            int unpack, int32_t* err, cudaStream_t st);                  \
   void launch_wss_##P(const WssArgs& wa, cudaStream_t st);                                \
   void launch_flux_##P(const FluxArgs& fa, cudaStream_t st);
 

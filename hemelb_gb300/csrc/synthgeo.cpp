@@ -50,6 +50,97 @@ const int CX15[15] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
 const int CY15[15] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, -1, 1, -1, 1};
 const int CZ15[15] = {0, 0, 0, 0, 0, 1, -1, 1, -1, -1, 1, 1, -1, -1, 1};
 
+// Elementary functions of the generators, written with IEEE +, -, *, / and sqrt
+// only (this unit is compiled without floating-point contraction), so a seeded
+// geometry comes out bit for bit the same on every host: the C library's sin,
+// cos, exp and cbrt differ by an ulp between x86_64 and aarch64 builds, and one
+// flipped rejection test changes a whole random tree.  Methods: Cody-Waite
+// range reduction (W. J. Cody and W. Waite, Software Manual for the Elementary
+// Functions, 1980) with the constant split into parts whose products with small
+// multiples are exact, then the Taylor series of the reduced argument; the cube
+// root by Newton's iteration on a mantissa scaled into [0.5, 4).
+namespace det {
+template <int N>
+struct InvFactorials {
+  double c[N + 1];
+  constexpr InvFactorials() : c() {
+    c[0] = 1.0;
+    for (int n = 1; n <= N; ++n) c[n] = c[n - 1] / n;
+  }
+};
+constexpr InvFactorials<24> kInvFact{};
+
+inline double exp(double x) {
+  if (x != x) return x;
+  if (x > 709.0) return HUGE_VAL;
+  if (x < -745.0) return 0.0;
+  constexpr double kInvLn2 = 1.44269504088896338700e+00;
+  constexpr double kLn2Hi = 6.93147180369123816490e-01;  // ln 2 to 32 bits: k * hi is exact
+  constexpr double kLn2Lo = 1.90821492927058770002e-10;  // ln 2 - hi
+  const double k = std::floor(x * kInvLn2 + 0.5);
+  const double r = (x - k * kLn2Hi) - k * kLn2Lo;  // |r| <= ln 2 / 2 (+ rounding)
+  double p = kInvFact.c[16];
+  for (int n = 15; n >= 0; --n) p = p * r + kInvFact.c[n];
+  return std::ldexp(p, (int)k);
+}
+
+// sin and cos of r with |r| <= pi/4 (+ rounding), by their Taylor series
+inline double sin_reduced(double r) {
+  const double r2 = r * r;
+  double p = kInvFact.c[23];
+  for (int n = 21; n >= 1; n -= 2) p = p * -r2 + kInvFact.c[n];
+  return p * r;
+}
+inline double cos_reduced(double r) {
+  const double r2 = r * r;
+  double p = kInvFact.c[24];
+  for (int n = 22; n >= 0; n -= 2) p = p * -r2 + kInvFact.c[n];
+  return p;
+}
+// x = k pi/2 + r; pi/2 in three parts, the first two to 33 bits
+inline double reduce_half_pi(double x, int* quadrant) {
+  constexpr double kInvPio2 = 6.36619772367581382433e-01;
+  constexpr double kPio2A = 1.57079632673412561417e+00;
+  constexpr double kPio2B = 6.07710050630396597660e-11;
+  constexpr double kPio2C = 2.02226624879595063154e-21;
+  const double k = std::floor(x * kInvPio2 + 0.5);
+  *quadrant = (int)(((long long)k % 4 + 4) % 4);
+  return ((x - k * kPio2A) - k * kPio2B) - k * kPio2C;
+}
+inline double sin(double x) {
+  int q;
+  const double r = reduce_half_pi(x, &q);
+  switch (q) {
+    case 0: return sin_reduced(r);
+    case 1: return cos_reduced(r);
+    case 2: return -sin_reduced(r);
+    default: return -cos_reduced(r);
+  }
+}
+inline double cos(double x) {
+  int q;
+  const double r = reduce_half_pi(x, &q);
+  switch (q) {
+    case 0: return cos_reduced(r);
+    case 1: return -sin_reduced(r);
+    case 2: return -cos_reduced(r);
+    default: return sin_reduced(r);
+  }
+}
+inline double cbrt(double x) {
+  if (x == 0.0 || x != x) return x;
+  const double a = x < 0 ? -x : x;
+  int e;
+  double m = std::frexp(a, &e);  // a = m 2^e, m in [0.5, 1)
+  int e3 = e >= 0 ? e / 3 : -((-e + 2) / 3);
+  m = std::ldexp(m, e - 3 * e3);  // in [0.5, 4)
+  double y = 1.0;
+  for (int it = 0; it < 8; ++it) y = y - (y * y * y - m) / (3.0 * y * y);
+  const double r = std::ldexp(y, e3);
+  return x < 0 ? -r : r;
+}
+}  // namespace det
+
 struct Vec {
   double x, y, z;
 };
@@ -97,7 +188,7 @@ bool inside_shape(const Shape& s, Vec p) {
   // stenosed pipe along z from a.z to b.z, axis through (a.x, a.y)
   if (p.z < s.a.z || p.z > s.b.z) return false;
   double dz = p.z - s.zc;
-  double rr = s.r * (1.0 - s.depth * std::exp(-dz * dz / (2.0 * s.sigma * s.sigma)));
+  double rr = s.r * (1.0 - s.depth * det::exp(-dz * dz / (2.0 * s.sigma * s.sigma)));
   double dx = p.x - s.a.x, dy = p.y - s.a.y;
   return dx * dx + dy * dy < rr * rr;
 }
@@ -118,7 +209,7 @@ bool shape_normal(const Shape& s, Vec p, double& sd, Vec& n) {
     return true;
   }
   const double dz = p.z - s.zc;
-  const double g = std::exp(-dz * dz / (2.0 * s.sigma * s.sigma));
+  const double g = det::exp(-dz * dz / (2.0 * s.sigma * s.sigma));
   const double R = s.r * (1.0 - s.depth * g);
   const double dRdz = s.r * s.depth * g * dz / (s.sigma * s.sigma);
   const double dx = p.x - s.a.x, dy = p.y - s.a.y, rho = std::sqrt(dx * dx + dy * dy);
@@ -483,8 +574,8 @@ Vec deflect(Vec dir, double theta, double phi) {
   Vec helper = std::fabs(dir.x) < 0.9 ? Vec{1, 0, 0} : Vec{0, 1, 0};
   Vec e1 = normalised(cross(dir, helper));
   Vec e2 = cross(dir, e1);
-  Vec lat = add(mul(e1, std::cos(phi)), mul(e2, std::sin(phi)));
-  return normalised(add(mul(dir, std::cos(theta)), mul(lat, std::sin(theta))));
+  Vec lat = add(mul(e1, det::cos(phi)), mul(e2, det::sin(phi)));
+  return normalised(add(mul(dir, det::cos(theta)), mul(lat, det::sin(theta))));
 }
 
 int finish(Geometry* g, int n_threads, void** handle) {
@@ -544,7 +635,7 @@ int hlbg_synth_bifurcation(uint64_t seed, double parent_radius, double parent_le
   std::uniform_real_distribution<double> U(0.0, 1.0);
   double split = 0.3 + 0.4 * U(rng);
   double half = (25.0 + 35.0 * U(rng)) * M_PI / 180.0;
-  double r1 = parent_radius * std::cbrt(split), r2 = parent_radius * std::cbrt(1.0 - split);
+  double r1 = parent_radius * det::cbrt(split), r2 = parent_radius * det::cbrt(1.0 - split);
   auto* g = new Geometry();
   g->q = q;
   g->with_cuts = with_cuts != 0;
@@ -552,7 +643,7 @@ int hlbg_synth_bifurcation(uint64_t seed, double parent_radius, double parent_le
   g->shapes.push_back(cyl(a, b, parent_radius, false, true));
   g->inlets.push_back(mk_iolet(0, 0, a, {0, 0, 1}, parent_radius));
   double ld = daughter_length_factor * parent_length;
-  Vec d1{std::sin(half), 0, std::cos(half)}, d2{-std::sin(half), 0, std::cos(half)};
+  Vec d1{det::sin(half), 0, det::cos(half)}, d2{-det::sin(half), 0, det::cos(half)};
   Vec e1 = add(b, mul(d1, ld)), e2 = add(b, mul(d2, ld));
   g->shapes.push_back(cyl(b, e1, r1, true, false));
   g->shapes.push_back(cyl(b, e2, r2, true, false));
@@ -618,7 +709,7 @@ int hlbg_synth_tree(uint64_t seed, int32_t box_sites, int32_t n_roots, int32_t d
         continue;
       }
       double split = 0.3 + 0.4 * U(rng);
-      double r1 = s.r * std::cbrt(split), r2 = s.r * std::cbrt(1.0 - split);
+      double r1 = s.r * det::cbrt(split), r2 = s.r * det::cbrt(1.0 - split);
       double phi = 2 * M_PI * U(rng);
       double th1 = (20.0 + 50.0 * U(rng)) * M_PI / 180.0;
       double th2 = (20.0 + 50.0 * U(rng)) * M_PI / 180.0;
@@ -1176,7 +1267,7 @@ int hlbg_synth_vessel_box(uint64_t seed, int32_t box_sites, int32_t kind, int32_
     const double split = 0.3 + 0.4 * U(rng);
     const double th1 = (20.0 + 25.0 * U(rng)) * M_PI / 180.0, th2 = (20.0 + 25.0 * U(rng)) * M_PI / 180.0;
     const double phi = 2.0 * M_PI * U(rng);
-    const double r1 = r0 * std::cbrt(split), r2 = r0 * std::cbrt(1.0 - split);
+    const double r1 = r0 * det::cbrt(split), r2 = r0 * det::cbrt(1.0 - split);
     const Vec a{axis0.x, axis0.y, z_in - 1.0}, b{axis0.x, axis0.y, zs};
     g->shapes.push_back(cyl(a, b, r0, false, true));
     g->inlets.push_back(mk_iolet(0, 0, {axis0.x, axis0.y, z_in}, {0, 0, 1}, r0));
@@ -1227,7 +1318,7 @@ int hlbg_synth_distance(void* handle, float* out) {
             sd = s.r - std::sqrt(dot(c, c));
           } else {
             const double dz = p.z - s.zc;
-            const double rr = s.r * (1.0 - s.depth * std::exp(-dz * dz / (2.0 * s.sigma * s.sigma)));
+            const double rr = s.r * (1.0 - s.depth * det::exp(-dz * dz / (2.0 * s.sigma * s.sigma)));
             const double dx = p.x - s.a.x, dy = p.y - s.a.y;
             sd = rr - std::sqrt(dx * dx + dy * dy);
           }

@@ -317,6 +317,10 @@ class LBM:
             check(rc, self._ctx)
         return a.value, b.value, d.value, rc
 
+    def SetMonitorInterval(self, interval: int):
+        """StabilityTester check every `interval` steps in StepMonitored (default 1)."""
+        check(self._lib.hlbg_set_monitor_interval(self._ctx, interval), self._ctx)
+
     def StepMonitored(self, n: int = 1) -> capi.Stats:
         """n steps with the fused StabilityTester; the stats of the step before the last
         (time_step -1 when there is none yet)."""

@@ -416,20 +416,28 @@ def generate(samples, box: int, average: bool = True, workers: int = 8, log=None
 
 def train(net: UNet, grids: Grids, n: int, batch: int = 4, seconds: float = 600.0,
           max_epochs: int = 1000, lr_max: float = 1e-3, lr_min: float = 2e-5, seed: int = 0,
-          augment: bool = True, log=None):
+          augment: bool = True, log=None, epochs: int | None = None):
     """Adam on the masked MSE of the normalised targets, cosine learning-rate decay
-    over the time budget, each batch under a random symmetry of the x-y plane when
-    `augment`.  Returns the loss history (per epoch mean)."""
+    over the time budget (or, with `epochs`, over that many epochs regardless of
+    time, so that the result does not depend on the machine's speed), each batch
+    under a random symmetry of the x-y plane when `augment`.  Returns the loss
+    history (per epoch mean)."""
     rng = np.random.default_rng(seed)
     hist = []
     t0 = time.perf_counter()
     epoch = 0
     done = False
+    per_epoch = max(1, (n - batch) // batch + 1)
+    if epochs is not None:
+        max_epochs = epochs
     while not done and epoch < max_epochs:
         order = rng.permutation(n)
         tot, cnt = 0.0, 0
         for k in range(0, n - batch + 1, batch):
-            frac = min(1.0, (time.perf_counter() - t0) / seconds)
+            if epochs is not None:
+                frac = (epoch * per_epoch + cnt) / float(epochs * per_epoch)
+            else:
+                frac = min(1.0, (time.perf_counter() - t0) / seconds)
             lr = lr_min + 0.5 * (lr_max - lr_min) * (1.0 + math.cos(math.pi * frac))
             idx = order[k:k + batch]
             code = int(rng.integers(8)) if augment else 0
@@ -443,7 +451,7 @@ def train(net: UNet, grids: Grids, n: int, batch: int = 4, seconds: float = 600.
             net.step(lr)
             tot += loss
             cnt += 1
-            if time.perf_counter() - t0 > seconds:
+            if epochs is None and time.perf_counter() - t0 > seconds:
                 done = True
                 break
         epoch += 1

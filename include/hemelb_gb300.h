@@ -256,8 +256,16 @@ int hlbg_run_to_steady(hlbg_ctx *ctx, double tol, double u_ref, int64_t max_step
  * the check), or time_step = -1 when there is none yet: the first step after the
  * distributions were set or changed outside a monitored step only records.
  * Replaces hlbg_step + hlbg_reduce per step without re-reading both arrays
- * (Code/lb/StabilityTester.h:91-183). */
+ * (Code/lb/StabilityTester.h:91-183).
+ * With a check interval K > 1 (hlbg_set_monitor_interval) only the steps t with
+ * t % K == 0 check; the step before each records the velocities and the others run
+ * the plain update, so the stats are those of the last check (time_step = its t,
+ * or -1 when none was made).  The reference checks on the cycle of its phased
+ * broadcast: every step on one rank, every 2 * tree-depth steps on many ranks
+ * (net::PhasedBroadcastRegular, Code/net/PhasedBroadcastRegular.h:106-182).
+ * K = 1 (the default) checks every step as described above. */
 int hlbg_step_monitored(hlbg_ctx *ctx, int32_t nsteps, hlbg_stats *out);
+int hlbg_set_monitor_interval(hlbg_ctx *ctx, int32_t interval);
 /* Mass flux through each iolet of the current state: out[k] (inlets first, then
  * outlets; n = their total) sums, over the sites with links to that iolet, the
  * site's momentum sum_d c_d f_d along the iolet's normalised inward normal, in
@@ -272,7 +280,9 @@ int hlbg_iolet_flux(hlbg_ctx *ctx, double *out, int32_t n);
  * and LocalDistributionInput reads them (LocalDistributionInput.cc:56-251).
  * hlbg_write_checkpoint writes the current state (the reference's fOld) at
  * `timestep`; with append != 0 it adds a record to an existing file of the same
- * geometry.  hlbg_read_checkpoint loads the record of `timestep` (the last one when
+ * geometry, and refuses (HLBG_ERR_INVAL, file unchanged) a timestep that is not
+ * larger than the file's last, since the reader finds a timestep by binary search
+ * over records in increasing order.  hlbg_read_checkpoint loads the record of `timestep` (the last one when
  * timestep < 0) into both time levels after checking every site's position, and
  * reports the timestep it found. */
 int hlbg_write_checkpoint(hlbg_ctx *ctx, const char *path, uint64_t timestep, double voxel_size,
@@ -335,8 +345,11 @@ int hlbg_put_f_device(hlbg_ctx *ctx, const double *dev, int32_t which);
 /* Density and velocity per site (contiguous order) from the current f. */
 int hlbg_get_macro(hlbg_ctx *ctx, double *rho, double *u);
 
-/* Reductions over the current state (mass, max|du| against the previous call's
- * velocity, min f, unstable count).  Synchronous. */
+/* StabilityTester reductions over the two time levels the context holds: mass
+ * and min f of the current distributions, unstable-site count (f <= 0 or not
+ * finite), and max|du| between the velocity of the current and of the previous
+ * time level (the last step's input), so a call depends on no earlier call.
+ * Synchronous.  Allocates its partial-sum buffer on its first call. */
 int hlbg_reduce(hlbg_ctx *ctx, hlbg_stats *out);
 
 /* Allocation-free variant of hlbg_reduce.  No counterpart in the reference: it
@@ -346,11 +359,16 @@ int hlbg_reduce(hlbg_ctx *ctx, hlbg_stats *out);
  * overlapped work -- whereas hlbg_reduce allocates its partial-sum buffer on its
  * first call.  Scratch is a fixed 2 MiB static device array (one partial per
  * 256-slot reduction block), so geometries are limited to HLBG_NOALLOC_MAX_SLOTS
- * slots (hlbg_slot_count); larger ones are rejected with HLBG_ERR_INVAL.  The
- * first call on a device (with that device current) looks up the array's device
- * address; make that first call before any stream capture.  All calls on a
- * device share the array: calls that overlap on the GPU race.  Synchronous, same
- * results as hlbg_reduce. */
+ * slots (hlbg_slot_count); larger ones are rejected with HLBG_ERR_INVAL.
+ * The array is placed on a GPU when the library's device code first loads there:
+ * at library load, or -- with lazy module loading, CUDA's default -- during the
+ * first hlbg_create on that device, which also looks up the array's device
+ * address (with the device current) and loads the reduction kernels, so no call
+ * of this function loads or allocates anything.  Every GPU that has held a
+ * context keeps the 2 MiB until the process exits.  A context does not survive a
+ * reset of its device (cudaDeviceReset); contexts created afterwards look the
+ * array up again.  All calls on a device share the array: calls that overlap on
+ * the GPU race.  Synchronous, same results as hlbg_reduce. */
 #define HLBG_NOALLOC_MAX_SLOTS (65536LL * 256LL)
 int hlbg_reduce_noalloc(hlbg_ctx *ctx, hlbg_stats *out);
 
@@ -364,6 +382,66 @@ int hlbg_time_steps(hlbg_ctx *ctx, int32_t nsteps, float *ms);
 /* Same as hlbg_step(nsteps) with events around every launch: summed device time
  * of the stream-and-collide launches and of the BFL PostStep launches (ms). */
 int hlbg_time_kernels(hlbg_ctx *ctx, int32_t nsteps, float *collide_ms, float *post_ms);
+
+/* ---- multi-rank halo: host-side index maps --------------------------------
+ * Splits one geometry over ranks for a device update per rank with one exchange
+ * per step, in place of the reference's domain decomposition and
+ * geometry::FieldData::SendAndReceive / CopyReceived (Code/geometry/FieldData.cc:
+ * 27-49) with lb::LBM's edge-first / mid-second order (Code/lb/lb.hpp:176-309).
+ * Host work only: no device memory, no CUDA call.
+ *
+ * hlbg_halo_partition: rank of every input block (block_rank[n_blocks]):
+ *   contiguous ranges of the device block order (z-columns: 2-D Morton order of
+ *   the block's (x, y), then z) cut where the running fluid-site count passes
+ *   k*N/n_ranks.  Any other assignment may be passed to hlbg_halo_create.
+ * hlbg_halo_create: the index maps of `rank`.  Its local geometry holds the owned
+ *   blocks, then every block of another rank that neighbours an owned block
+ *   (ghost blocks), with their link records, so an owned site sees the same
+ *   neighbourhood as in the whole geometry; a context created on it updates the
+ *   owned sites exactly as the whole geometry's context would once the received
+ *   distributions are in place.  Per peer, two lists of (local block, direction,
+ *   in-block site) triples: send = the distributions this rank's owned sites
+ *   stream into the peer's sites (found in this rank's new distributions at the
+ *   ghost sites), receive = those the peer streams into this rank's sites.  A
+ *   send list and the peer's receive list name the same distributions in the same
+ *   order (ascending target block, site, direction of the input geometry).
+ *   Exchange after StreamAndCollide, before PostStep.  D3Q19 only.
+ * hlbg_halo_edge_blocks: per owned block, 1 when one of its sites streams into a
+ *   ghost block (update these first and send; update the others meanwhile).
+ * hlbg_halo_block_source: input block index of every local block.
+ * The halo owns the arrays of its local geometry view; the view is valid until
+ * hlbg_halo_destroy.  Errors: HLBG_ERR_INVAL with hlbg_halo_last_error. */
+typedef struct hlbg_halo hlbg_halo;
+int hlbg_halo_partition(const hlbg_geometry *g, int32_t n_ranks, int32_t *block_rank);
+int hlbg_halo_create(const hlbg_geometry *g, const int32_t *block_rank, int32_t n_ranks, int32_t rank,
+                     hlbg_halo **out);
+void hlbg_halo_destroy(hlbg_halo *h);
+const char *hlbg_halo_last_error(const hlbg_halo *h);
+int hlbg_halo_local_geometry(const hlbg_halo *h, hlbg_geometry *out, int64_t *n_owned_blocks);
+int hlbg_halo_block_source(const hlbg_halo *h, int64_t *input_block);
+int hlbg_halo_edge_blocks(const hlbg_halo *h, uint8_t *is_edge);
+int32_t hlbg_halo_peer_count(const hlbg_halo *h);
+int hlbg_halo_peer(const hlbg_halo *h, int32_t k, int32_t *peer_rank, int64_t *n_send, int64_t *n_recv);
+int hlbg_halo_list(const hlbg_halo *h, int32_t k, int32_t is_recv, int32_t *local_block, int8_t *direction,
+                   int16_t *site);
+
+/* Device half of the exchange, for a context created on a halo's local geometry.
+ * hlbg_halo_offsets: element offsets, in the context's distribution arrays, of
+ *   (block, direction, in-block site) triples, block indexing the geometry given
+ *   to hlbg_create (for a halo's lists: its local blocks).  Host work.
+ * hlbg_halo_pack_device / hlbg_halo_unpack_device: copy the new distributions
+ *   (the state StreamAndCollide wrote, before PostStep and the swap) at device
+ *   `offsets` into / from a device buffer of n elements of the storage type
+ *   (hlbg_storage_bytes: 8 FP64, 4 FP32-deviation, 2 FP16), so the exchange is
+ *   exact in every form.  Enqueued on the context stream; offsets outside the
+ *   arrays are skipped and reported by the next hlbg_halo_check (which
+ *   synchronises the stream). */
+int hlbg_halo_offsets(hlbg_ctx *ctx, const int32_t *block, const int8_t *direction, const int16_t *site,
+                      int64_t n, int64_t *out);
+int hlbg_halo_pack_device(hlbg_ctx *ctx, const int64_t *offsets, int64_t n, void *buf);
+int hlbg_halo_unpack_device(hlbg_ctx *ctx, const int64_t *offsets, int64_t n, const void *buf);
+int hlbg_halo_check(hlbg_ctx *ctx);
+int hlbg_storage_bytes(const hlbg_ctx *ctx);
 
 /* Library build string. */
 const char *hlbg_version(void);

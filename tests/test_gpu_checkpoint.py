@@ -38,6 +38,13 @@ def test_checkpoint_bytes_offsets_append_and_restart(tmp_path, precision):
     f13 = s.GetFOld()
     _, recs = X.read_checkpoint(open(path, "rb").read())
     assert [r[0] for r in recs] == [9, 13]
+    # the reader's binary search needs increasing timesteps: an append that would
+    # repeat or go back is refused and leaves the file as it was
+    before = open(path, "rb").read()
+    for t in (13, 11, 0):
+        with pytest.raises(RuntimeError, match="does not follow"):
+            s.WriteCheckpoint(path, t, voxel_size=0.3e-3, origin=ORIGIN, append=True)
+    assert open(path, "rb").read() == before
     assert np.array_equal(recs[1][2], f13) and np.array_equal(recs[1][1], coords)
     # restart from step 9 in a fresh solver: both time levels hold the record,
     # and four more steps reproduce the original run bit for bit

@@ -135,3 +135,35 @@ def test_incompressibility_checker_of_the_monitored_state(prec):
     assert abs(a.MaxMachNumber() - inc.max_velocity * np.sqrt(3.0)) <= 1e-15
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32DEV])
+@pytest.mark.parametrize("interval", [3, 6])
+def test_monitor_interval_checks_every_kth_step(prec, interval):
+    """With a check interval K the StabilityTester checks the steps t with
+    t % K == 0 (the step before records the velocities, the others run the plain
+    update): the stats of each check equal the separate reduction after the same
+    step, and the state equals plain stepping (monitoring changes no distribution)."""
+    g, case, ur = _small_case(0)
+    a = case.solver(prec)
+    b = case.solver(prec)
+    a.SetInitialConditions()
+    b.SetInitialConditions()
+    a.SetMonitorInterval(interval)
+    last = -1
+    for t in range(1, 5 * interval + 2):
+        # step t collides the state after t - 1 steps, which b holds now
+        sb = b.reduce() if t % interval == 0 else None
+        sa = a.StepMonitored(1)
+        b.DoTimeStep(1)
+        if sb is not None:
+            last = t
+            assert sa.time_step == sb.time_step == t
+            if prec == capi.FP64:
+                assert sa.max_du == sb.max_du and sa.min_f == sb.min_f
+            else:
+                assert abs(sa.max_du - sb.max_du) <= 1e-5 * sb.max_du + 1e-12
+        assert sa.time_step == last  # stats of the last check made
+    assert np.array_equal(a.GetFOld(), b.GetFOld())
+    a.close()
+    b.close()

@@ -10,6 +10,10 @@ collected last so that a run stopping at the first failure has run every other
 test already.
 """
 import ctypes as C
+import json
+import os
+import subprocess
+import sys
 
 import pytest
 
@@ -18,6 +22,7 @@ from hemelb_gb300 import capi, cases
 pytestmark = pytest.mark.gpu
 
 REL = 1e-12  # tolerance of the reduction checks in tests/test_gpu_parity.py
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _close(a, b):
@@ -77,3 +82,45 @@ def test_noalloc_reduce_rejects_geometries_above_its_limit():
     assert rc == capi.HLBG_ERR_INVAL
     assert b"exceed its limit" in lib.hlbg_last_error(s.ctx)
     s.close()
+
+
+_FREE_BYTES_SCRIPT = r"""
+import ctypes as C, json, sys
+sys.path.insert(0, sys.argv[1])
+from hemelb_gb300 import capi, cases
+lib = capi.load()
+cu = C.CDLL("libcuda.so.1")
+cu.cuMemGetInfo_v2.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+
+def free_bytes():
+    f, t = C.c_size_t(), C.c_size_t()
+    assert cu.cuMemGetInfo_v2(C.byref(f), C.byref(t)) == 0
+    return f.value
+
+c = cases.pipe(radius=6.0, length=30)
+s = c.solver(capi.FP32DEV)
+s.SetInitialConditions()
+s.DoTimeStep(5)
+before = free_bytes()
+rcs = []
+for _ in range(4):
+    st = capi.Stats()
+    rcs.append(lib.hlbg_reduce_noalloc(s.ctx, C.byref(st)))
+    s.DoTimeStep(1)
+after = free_bytes()
+print(json.dumps({"before": before, "after": after, "rcs": rcs}))
+"""
+
+
+def test_noalloc_reduce_takes_no_device_memory_under_lazy_loading():
+    """With lazy module loading the library's device code is placed on the GPU on
+    first use; the context's creation must have done that for the static scratch
+    array, so the first hlbg_reduce_noalloc call (and every later one) leaves the
+    device's free memory unchanged.  Fresh process, CUDA_MODULE_LOADING=LAZY."""
+    env = dict(os.environ, CUDA_MODULE_LOADING="LAZY")
+    r = subprocess.run([sys.executable, "-c", _FREE_BYTES_SCRIPT, ROOT], env=env, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["rcs"] == [capi.HLBG_OK] * 4
+    assert out["after"] == out["before"], out
