@@ -2,8 +2,8 @@
 """Benchmark of the GB300 lattice-Boltzmann update (fluid MLUPS, % of HBM roofline).
 
 Workload (default): seeded random vascular forest in a 1280^3 box of sparse 8^3
-blocks (5 trees of depth 7, root radius 60, Murray radii, branch angles 20-70
-degrees, segment length 6-10 x radius), about 190M fluid sites; D3Q19 TRT
+blocks (6 trees of depth 7, root radius 60, Murray radii, branch angles 20-70
+degrees, segment length 6-10 x radius), 222,966,063 fluid sites; D3Q19 TRT
 (Lambda = 3/16), simple bounce-back walls, Nash pressure inlets at density 1.001
 and outlets at 1.0, distributions stored as FP32 deviations from the rest
 weights.  A "step" is one full LB time step over every fluid site.  The
@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--workload", default="tree", choices=["tree", "pipe", "bifurcation"])
-    ap.add_argument("--roots", type=int, default=5)
+    ap.add_argument("--roots", type=int, default=6)
     ap.add_argument("--box", type=int, default=1280)
     ap.add_argument("--depth", type=int, default=7)
     ap.add_argument("--root-radius", type=float, default=60.0)
@@ -290,7 +290,8 @@ def main():
             print(json.dumps(reports.precision_report(steps=args.steps)), flush=True)
         elif args.report == "tree_precision":
             print(json.dumps(reports.tree_precision_report(steps=args.steps, roots=args.roots,
-                                                           box=args.box, depth=args.depth)), flush=True)
+                                                           box=args.box, depth=args.depth,
+                                                           root_radius=args.root_radius)), flush=True)
         elif args.report == "ensemble":
             print(json.dumps(reports.ensemble_report(args.members, steps=args.steps,
                                                      warmup=args.warmup)), flush=True)

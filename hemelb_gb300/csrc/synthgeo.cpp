@@ -692,7 +692,11 @@ int hlbg_synth_tree(uint64_t seed, int32_t box_sites, int32_t n_roots, int32_t d
     cxr = std::min(std::max(cxr, rr + margin + 2), B - rr - margin - 3);
     cyr = std::min(std::max(cyr, rr + margin + 2), B - rr - margin - 3);
     Vec start{cxr, cyr, margin};
-    Vec dir = deflect({0, 0, 1}, 10.0 * M_PI / 180.0 * U(rng), 2 * M_PI * U(rng));
+    // two draws in sequence: the order in which a call's arguments are evaluated is
+    // unspecified (it differs between the x86_64 and aarch64 compilers)
+    const double tilt = 10.0 * M_PI / 180.0 * U(rng);
+    const double azimuth = 2 * M_PI * U(rng);
+    Vec dir = deflect({0, 0, 1}, tilt, azimuth);
     g->inlets.push_back(mk_iolet(0, root, start, dir, rr));
     std::vector<Seg> stack{{start, dir, rr, 0}};
     while (!stack.empty()) {

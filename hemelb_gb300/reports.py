@@ -133,28 +133,44 @@ def ensemble_report(n_members: int = 512, steps: int = 50, warmup: int = 5, seed
             "speedup": (n * steps / batched_s) / (seq_sites * steps / seq_s)}
 
 
-def tree_precision_report(steps: int = 1000, roots: int = 5, box: int = 1280, depth: int = 7) -> dict:
-    """The forest workload (TRT, SBB, Nash) in FP64, FP32-deviation and FP16-storage
-    forms from rest for `steps` steps; velocity / pressure error of the reduced forms
-    against FP64 (FP64 is the oracle's arithmetic, bit-exact on the GPU)."""
-    case = cases.tree(n_roots=roots, box_sites=box, depth=depth, precision=capi.FP64)
-    out = {"workload": "forest of %d trees depth %d in %d^3, %d fluid sites, %d steps from rest, TRT"
-                       % (roots, depth, box, case.geometry.n_fluid, steps), "forms": {}}
-    ref = None
-    for name, prec in (("fp64", capi.FP64), ("fp32dev", capi.FP32DEV), ("fp16", capi.FP16)):
-        s = case.solver(prec)
-        s.SetInitialConditions()
-        t0 = time.perf_counter()
-        s.DoTimeStep(steps)
-        dt = time.perf_counter() - t0
-        rho, u = s.macro()
+def tree_precision_report(steps: int = 10000, roots: int = 1, box: int = 1280, depth: int = 7,
+                          root_radius: float = 60.0, checkpoints=None) -> dict:
+    """The forest generator's workload (TRT, SBB, Nash) in FP64, FP32-deviation and
+    FP16-storage forms from rest, stepped side by side; at each checkpoint the
+    velocity / pressure error of the reduced forms against FP64 (FP64 is the
+    oracle's arithmetic, bit-exact on the GPU).  The default is one tree of the
+    benchmark's forest (a cropped forest: the same generator and parameters) run
+    long enough for the flow to cross it."""
+    case = cases.tree(n_roots=roots, box_sites=box, depth=depth, root_radius=root_radius,
+                      precision=capi.FP64)
+    cps = sorted({int(c) for c in (checkpoints or [steps // 10, steps // 2, steps]) if 0 < c <= steps})
+    forms = (("fp64", capi.FP64), ("fp32dev", capi.FP32DEV), ("fp16", capi.FP16))
+    solvers = {}
+    for name, prec in forms:
+        solvers[name] = case.solver(prec)
+        solvers[name].SetInitialConditions()
+    n = solvers["fp64"].n_sites
+    out = {"workload": "forest of %d tree(s) depth %d (root radius %g) in %d^3, %d fluid sites, TRT, "
+                       "SBB walls, Nash inlet 1.001 / outlets 1.0, from rest"
+                       % (roots, depth, root_radius, box, n), "checkpoints": []}
+    secs = {name: 0.0 for name, _ in forms}
+    done = 0
+    for cp in cps:
+        for name, _ in forms:
+            t0 = time.perf_counter()
+            solvers[name].DoTimeStep(cp - done)
+            secs[name] += time.perf_counter() - t0
+        done = cp
+        rho_ref, u_ref = solvers["fp64"].macro()
+        umag = np.linalg.norm(u_ref, axis=1)
+        entry = {"step": cp, "u_peak": float(umag.max()), "u_mean": float(umag.mean())}
+        for name in ("fp32dev", "fp16"):
+            rho, u = solvers[name].macro()
+            entry[name] = _errors(rho, u, rho_ref, u_ref)
+            del rho, u
+        out["checkpoints"].append(entry)
+        del rho_ref, u_ref
+    out["mlups"] = {name: n * done / secs[name] / 1e6 for name, _ in forms}
+    for s in solvers.values():
         s.close()
-        entry = {"seconds": dt, "mlups": len(rho) * steps / dt / 1e6}
-        if ref is None:
-            ref = (rho, u)
-            entry["u_peak"] = float(np.linalg.norm(u, axis=1).max())
-        else:
-            entry.update(_errors(rho, u, *ref))
-        out["forms"][name] = entry
-        del rho, u
     return out

@@ -451,3 +451,22 @@ def test_set_iolets_is_creating_with_them():
         c.SetIolets(new.inlets, new_out[:-1])
     with pytest.raises(capi.HlbgError):
         c.SetIolets(new_out[:1], new_out)  # pressure iolet on the Ladd inlet streamer
+
+
+def test_tree_fp32_deviation_velocity_error_within_1e5_developed_flow():
+    """The forest generator's workload (TRT, SBB, Nash 1.001 / 1.0) on a small tree
+    (256^3 box, depth 5, root radius 12, about 0.46M sites), run until the flow has
+    developed (3000 steps: several viscous times R^2 / nu of the root segment):
+    the FP32-deviation velocity is within 1e-5 relative L2 of FP64, the bound the
+    FP32-deviation form is held to."""
+    c = cases.tree(seed=7, box_sites=256, n_roots=1, depth=5, root_radius=12.0, precision=capi.FP64)
+    a = c.solver(capi.FP64)
+    b = c.solver(capi.FP32DEV)
+    for s in (a, b):
+        s.SetInitialConditions()
+        s.DoTimeStep(3000)
+    _, ua = a.macro()
+    _, ub = b.macro()
+    assert np.linalg.norm(ua, axis=1).max() > 1e-4  # the flow is there
+    rel = np.linalg.norm(ub - ua) / np.linalg.norm(ua)
+    assert rel <= 1e-5, rel
