@@ -28,6 +28,7 @@ UNITS = [
     ("lb_fp32.cu", []),
     ("capi.cu", ["--fmad=false"]),
     ("nn_kernels.cu", []),
+    ("nn_tc.cu", []),
 ]
 HOST_UNITS = ["synthgeo.cpp", "halo.cpp"]
 

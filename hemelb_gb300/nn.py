@@ -57,6 +57,28 @@ def conv3d(x, w, bias, out, out_f32=None, taps=27, relu=False):
                               taps, int(relu), _stream()), "hlbg_nn_conv3d")
 
 
+def conv3d_tc(x, w, bias, out, out_f32=None, taps=27, relu=False):
+    """conv3d on the tcgen05 tensor cores (cin and cout multiples of 16, cout <= 256)."""
+    _need(x, _BF16, "conv3d input")
+    _need(w, _BF16, "conv3d weights")
+    _need(out, _BF16, "conv3d output")
+    n, d, h, wd, cin = x.shape
+    t, cout, cin_w = w.shape
+    if t != taps or cin_w != cin or out.shape != (n, d, h, wd, cout):
+        raise ValueError(f"conv3d shapes: x {tuple(x.shape)} w {tuple(w.shape)} out {tuple(out.shape)}")
+    if bias is not None:
+        _need(bias, _F32, "conv3d bias")
+    if out_f32 is not None:
+        _need(out_f32, _F32, "conv3d FP32 output")
+    _ok(_lib().hlbg_nn_conv3d_tc(_p(x), cin, _p(w), _p(bias), _p(out), _p(out_f32), cout, n, d, h, wd,
+                                 taps, int(relu), _stream()), "hlbg_nn_conv3d_tc")
+
+
+def tc_error(reset: bool = True) -> int:
+    """Nonzero when a bounded wait of a tcgen05 convolution gave up."""
+    return int(_lib().hlbg_nn_tc_error(int(reset)))
+
+
 def flip_transpose(w, wt):
     _need(w, _BF16, "weights")
     _need(wt, _BF16, "flipped weights")

@@ -23,6 +23,16 @@ extern "C" {
 int hlbg_nn_conv3d(const void *in, int32_t cin, const void *w, const float *bias, void *out,
                    float *out_f32, int32_t cout, int32_t n, int32_t d, int32_t h, int32_t wd,
                    int32_t taps, int32_t relu, void *stream);
+/* The same convolution on the fifth-generation tensor cores (tcgen05.mma, FP32
+ * accumulator in tensor memory, TMA-staged operands): cin a multiple of 16, cout
+ * a multiple of 16 up to 256, taps 27 or 1; in, w, out, out_f32 16-byte aligned.
+ * Returns 1 for shapes it does not take (hlbg_nn_conv3d takes every shape). */
+int hlbg_nn_conv3d_tc(const void *in, int32_t cin, const void *w, const float *bias, void *out,
+                      float *out_f32, int32_t cout, int32_t n, int32_t d, int32_t h, int32_t wd,
+                      int32_t taps, int32_t relu, void *stream);
+/* Nonzero when a bounded wait of a tcgen05 convolution gave up since the last
+ * reset (reset != 0 clears it); synchronous. */
+int hlbg_nn_tc_error(int32_t reset);
 /* dw[tap][co][ci] += sum over voxels of dy[m, co] * x[m + off(tap), ci] (FP32) */
 int hlbg_nn_conv3d_wgrad(const void *x, int32_t cin, const void *dy, int32_t cout, float *dw,
                          int32_t n, int32_t d, int32_t h, int32_t wd, int32_t taps, void *stream);

@@ -42,6 +42,34 @@ def test_conv_forward(cin, cout, taps, relu, shape):
     assert np.all(np.abs(y.float().cpu().numpy() - y32.cpu().numpy()) <= 2.0 ** -8 * np.abs(y32.cpu().numpy()) + 1e-30)
 
 
+@pytest.mark.parametrize("cin,cout,taps,relu,shape", [
+    (16, 16, 27, False, (2, 6, 5, 7)), (16, 32, 27, True, (2, 6, 5, 7)), (32, 48, 27, False, (1, 9, 12, 17)),
+    (48, 96, 27, True, (1, 13, 20, 24)), (96, 192, 27, False, (1, 8, 8, 16)), (288, 96, 27, True, (1, 8, 12, 12)),
+    (16, 64, 1, False, (2, 6, 5, 7)), (192, 256, 27, False, (1, 4, 4, 8))])
+def test_conv_forward_tcgen05(cin, cout, taps, relu, shape):
+    """The tcgen05 / TMEM / TMA convolution against the oracle and against the
+    mma.sync kernel: partial 8x4x4 bricks at every volume edge (TMA zero fill is the
+    padding), 1 to 18 channel slices per tap, N = 16 to 256."""
+    rng = np.random.default_rng(3 * cin + cout)
+    x, xt = bf16(rng.standard_normal(shape + (cin,)))
+    w, wt = bf16(rng.standard_normal((taps, cout, cin)) / np.sqrt(27 * cin))
+    b = rng.standard_normal(cout).astype(np.float32)
+    bt = torch.tensor(b, device="cuda")
+    y = torch.empty(shape + (cout,), dtype=torch.bfloat16, device="cuda")
+    y32 = torch.empty(shape + (cout,), dtype=torch.float32, device="cuda")
+    nn.tc_error(reset=True)
+    nn.conv3d_tc(xt, wt, bt, y, y32, taps=taps, relu=relu)
+    torch.cuda.synchronize()
+    assert nn.tc_error() == 0
+    ref = O.conv3d(x, w, b.astype(np.float64), relu=relu)
+    assert close(y32.cpu().numpy(), ref, 1e-4)
+    assert np.all(np.abs(y.float().cpu().numpy() - y32.cpu().numpy()) <= 2.0 ** -8 * np.abs(y32.cpu().numpy()) + 1e-30)
+    z32 = torch.empty_like(y32)
+    nn.conv3d(xt, wt, bt, torch.empty_like(y), z32, taps=taps, relu=relu)
+    torch.cuda.synchronize()
+    assert close(y32.cpu().numpy(), z32.cpu().numpy(), 1e-5)
+
+
 @pytest.mark.parametrize("cin,cout,shape", [(16, 32, (2, 6, 5, 4)), (32, 16, (2, 6, 5, 4)), (48, 48, (2, 6, 5, 4)),
                                              (32, 32, (2, 13, 20, 24)), (16, 48, (1, 9, 12, 17))])
 def test_conv_gradients(cin, cout, shape):
