@@ -342,12 +342,14 @@ def main():
     else:
         kname = KERNEL_OF_VARIANT.get(variant, "k_stream_collide").replace("<P", "<%d" % prec)
     base = kname.split("<")[0]
-    # DRAM bytes per site: a one-pass capture of this workload, else a small-case full capture
-    tps = profile_traffic("%s_%s_%s_dram" % (base, args.precision, args.workload)) \
-        or profile_traffic("%s_%s_%s" % (base, args.precision, args.workload))
+    # DRAM bytes per site from the ncu capture of one launch of this kernel on a small
+    # case of the same generator (one tree in a 512^3 box, root radius 50, depth 6:
+    # 16.9M sites, 10.5% boundary sites against the forest's 9.6%), scaled by sites
+    tps = profile_traffic("%s_%s_%s" % (base, args.precision, args.workload))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": (tps * n if tps is not None else None),
+                "traffic_source": "ncu dram bytes per site of a small case of the same generator, x sites",
                 "algorithmic_bytes_per_launch": B_ALG[prec] * n,
                 "kernel": "hlbg::" + kname, "launch_ms": per_launch}
     # ---- end to end through the C ABI: per step, H2D of that step's iolet values,

@@ -198,6 +198,65 @@ struct PushAll<P, Q> {
   static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int, int, int, const T*) {}
 };
 
+// HLBG_PUSH_PRECOMP=1: the bulk pushes take each axis's wrapped neighbour
+// coordinates and neighbour-table offsets from values computed once per site
+// (default layout only: identity in-block order, no packed blocks).
+#ifndef HLBG_PUSH_PRECOMP
+#define HLBG_PUSH_PRECOMP 0
+#endif
+struct PushGeo {
+  int tx_m, tx_0, tx_p, ty_m, ty_0, ty_p, tz_m, tz_0, tz_p;  // slot bits of x-1, x, x+1 (wrapped), ...
+  int kx_m, kx_p, ky_m, ky_p, kz_m, kz_p;                       // table-index steps at block faces
+  __device__ __forceinline__ PushGeo(int x, int y, int z) {
+    tx_0 = x << 6;
+    tx_m = ((x - 1) & 7) << 6;
+    tx_p = ((x + 1) & 7) << 6;
+    ty_0 = y << 3;
+    ty_m = ((y - 1) & 7) << 3;
+    ty_p = ((y + 1) & 7) << 3;
+    tz_0 = z;
+    tz_m = (z - 1) & 7;
+    tz_p = (z + 1) & 7;
+    kx_m = x == 0 ? -9 : 0;
+    kx_p = x == 7 ? 9 : 0;
+    ky_m = y == 0 ? -3 : 0;
+    ky_p = y == 7 ? 3 : 0;
+    kz_m = z == 0 ? -1 : 0;
+    kz_p = z == 7 ? 1 : 0;
+  }
+  template <int C>
+  __device__ __forceinline__ int tx() const { return C < 0 ? tx_m : (C > 0 ? tx_p : tx_0); }
+  template <int C>
+  __device__ __forceinline__ int ty() const { return C < 0 ? ty_m : (C > 0 ? ty_p : ty_0); }
+  template <int C>
+  __device__ __forceinline__ int tz() const { return C < 0 ? tz_m : (C > 0 ? tz_p : tz_0); }
+  template <int C>
+  __device__ __forceinline__ int kx() const { return C < 0 ? kx_m : (C > 0 ? kx_p : 0); }
+  template <int C>
+  __device__ __forceinline__ int ky() const { return C < 0 ? ky_m : (C > 0 ? ky_p : 0); }
+  template <int C>
+  __device__ __forceinline__ int kz() const { return C < 0 ? kz_m : (C > 0 ? kz_p : 0); }
+};
+
+template <int P, int D>
+struct PushBulkG {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, const PushGeo& g,
+                                             bool store, const T* fpost) {
+    constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
+    const int k = 13 + g.kx<cx>() + g.ky<cy>() + g.kz<cz>();
+    const int tl = g.tx<cx>() | g.ty<cy>() | g.tz<cz>();
+    const int32_t e = base(k);  // every lane shuffles
+    if (store) Store<P>::store(fn, (int64_t)e * (Q * kSites) + (D * kSites + tl), fpost[D], a);
+    PushBulkG<P, D + 1>::run(fn, a, base, g, store, fpost);
+  }
+};
+template <int P>
+struct PushBulkG<P, Q> {
+  template <class S, class T, class B>
+  static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, const PushGeo&, bool, const T*) {}
+};
+
 // Pushes of the all-slots kernel: every lane takes part in the shuffles, only
 // bulk sites store.
 template <int P, int D>
@@ -610,7 +669,11 @@ __device__ __forceinline__ void collide_and_push(const StepArgs& a, int64_t b, i
   const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
   const bool bnd = code >= 2;
   if (__ballot_sync(0xffffffffu, bnd) == 0) {
+#if HLBG_PUSH_PRECOMP && !HLBG_PACK && !HLBG_BLOCK_ORDER
+    PushBulkG<P, 0>::run(fn, a, ShflBase{tabreg}, PushGeo(x, y, z), code == 1, fpost);
+#else
     PushBulk<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, code == 1, fpost);
+#endif
   } else {
     const int64_t r = bnd ? (int64_t)code - 2 : 0;
     const uint64_t links = bnd ? a.b_links[r] : 0ull;
@@ -833,144 +896,13 @@ void launch_block_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st
     k_stream_collide_block<P, THREADS, MINB><<<(unsigned)a.n_blocks, THREADS, smem, st>>>(a, bxyz);
 }
 
-// Fluid list with UNITS consecutive units per warp: the warp loads the next unit's
-// list entries while it collides and pushes the current one, so only its first
-// unit waits on a list load before its distributions.  HLBG_LIST_UNITS (default 1:
-// one unit per warp, k_stream_collide_listed) selects it for plain steps.
-#ifndef HLBG_LIST_UNITS
-#define HLBG_LIST_UNITS 1
-#endif
 // Resident CTAs per SM of the 128-thread fluid-list launch (variant 6) in plain steps.
 #ifndef HLBG_LIST_MINB
 #define HLBG_LIST_MINB 8
 #endif
-template <int P, int THREADS, int MINB, int UNITS>
-__global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed_multi(StepArgs a,
-                                                                               const int32_t* block_xyz) {
-  MonAccT<P> acc = mon_neutral_t<P>();
-  const int64_t w0 = (((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5) * UNITS;
-  if (w0 >= a.n_warps) return;  // whole warp
-  const int lane = threadIdx.x & 31;
-  int32_t e = __ldg(a.warp_block + w0);
-  unsigned js = __ldg(a.lane_slot + w0 * 32 + lane);
-#pragma unroll 1
-  for (int u = 0; u < UNITS; ++u) {
-    const int64_t wn = w0 + u + 1;
-    const bool more = u + 1 < UNITS && wn < a.n_warps;  // the same for the whole warp
-    int32_t en = 0;
-    unsigned jn = 0xffffu;
-    if (more) {
-      en = __ldg(a.warp_block + wn);
-      jn = __ldg(a.lane_slot + wn * 32 + lane);
-    }
-    collide_listed_unit<P, false>(a, e, js, block_xyz, acc, false);
-    if (!more) break;
-    e = en;
-    js = jn;
-  }
-}
-
-// The same with each lane's distributions of the next unit staged in shared memory
-// by cp.async while the current unit collides and pushes (data in flight holds no
-// registers), and the list entries loaded two units ahead.  FP32 and FP64 storage
-// (cp.async copies 4, 8 or 16 bytes).  HLBG_LIST_STAGE=1 selects it.
-#ifndef HLBG_LIST_STAGE
-#define HLBG_LIST_STAGE 0
-#endif
-template <int P>
-__device__ __forceinline__ void stage_unit(const StepArgs& a, int32_t e, unsigned js, uint32_t dst) {
-  using S = typename Store<P>::S;
-  if (e < 0 || js == 0xffffu) return;
-  const int64_t b = e & 0x7fffffff;
-  const S* fo = static_cast<const S*>(a.f_old) + b * (Q * kSites) + (js & (kSites - 1));
-#pragma unroll
-  for (int d = 0; d < Q; ++d) {
-    if constexpr (sizeof(S) == 4)
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst + d * 32 * 4), "l"(fo + d * kSites) : "memory");
-    else
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst + d * 32 * 8), "l"(fo + d * kSites) : "memory");
-  }
-}
-
-template <int P, int THREADS, int MINB, int UNITS>
-__global__ void __launch_bounds__(THREADS, MINB) k_stream_collide_listed_staged(StepArgs a,
-                                                                                const int32_t* block_xyz) {
-  using S = typename Store<P>::S;
-  using T = typename Calc<P>::T;
-  __shared__ S stage[THREADS / 32][2][Q][32];
-  MonAccT<P> acc = mon_neutral_t<P>();
-  MonOld<P> uo;
-  const int64_t w0 = (((int64_t)blockIdx.x * THREADS + threadIdx.x) >> 5) * UNITS;
-  if (w0 >= a.n_warps) return;  // whole warp
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const uint32_t buf0 = (uint32_t)__cvta_generic_to_shared(&stage[wib][0][0][lane]);
-  const uint32_t buf_step = (uint32_t)(Q * 32 * sizeof(S));
-  int32_t e = __ldg(a.warp_block + w0);
-  unsigned js = __ldg(a.lane_slot + w0 * 32 + lane);
-  stage_unit<P>(a, e, js, buf0);
-  asm volatile("cp.async.commit_group;" ::: "memory");
-  const bool has1 = UNITS > 1 && w0 + 1 < a.n_warps;
-  int32_t e1 = has1 ? __ldg(a.warp_block + w0 + 1) : -1;
-  unsigned js1 = has1 ? __ldg(a.lane_slot + (w0 + 1) * 32 + lane) : 0xffffu;
-#pragma unroll 1
-  for (int u = 0; u < UNITS; ++u) {
-    const int64_t w = w0 + u;
-    if (w >= a.n_warps) break;  // the same for the whole warp
-    const bool has2 = u + 2 < UNITS && w + 2 < a.n_warps;
-    const int32_t e2 = has2 ? __ldg(a.warp_block + w + 2) : -1;
-    const unsigned js2 = has2 ? __ldg(a.lane_slot + (w + 2) * 32 + lane) : 0xffffu;
-    if (u + 1 < UNITS) stage_unit<P>(a, e1, js1, buf0 + ((u + 1) & 1) * buf_step);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    asm volatile("cp.async.wait_group 1;" ::: "memory");  // this lane's copies of unit u
-    const int64_t b = e & 0x7fffffff;
-    S* fn = static_cast<S*>(a.f_new);
-    const bool on = js != 0xffffu;
-    const int j = on ? (int)(js & (kSites - 1)) : 0;
-    const int64_t s = b * kSites + j;
-    if (e < 0) {  // zero-fill unit
-      if (on) {
-#pragma unroll
-        for (int d = 0; d < Q; ++d) Store<P>::store(fn, fidx(s, d), (T)0, a);
-      }
-    } else {
-      const int32_t* tab = a.block_nbr + b * 27;
-      const int32_t tabreg = lane < 27 ? __ldg(tab + lane) : 0;
-      const uint32_t code = on ? ((js & kListBoundary) ? a.site_code[s] : 1u) : 0u;
-      const bool packed = (__shfl_sync(0xffffffffu, tabreg, 13) & kPackedBit) != 0;
-      const int l = on ? site_of_slot(a, s, packed) : 0;
-      T f[Q];
-      const S* sf = &stage[wib][u & 1][0][lane];
-      if (on) {
-#pragma unroll
-        for (int i = 0; i < Q; ++i) f[i] = Store<P>::load(sf, i * 32, a);
-      } else {
-#pragma unroll
-        for (int i = 0; i < Q; ++i) f[i] = (T)(P == 0 ? weight_d(i) : 0.0);
-      }
-      collide_and_push<P, false>(a, b, j, s, l, code, tabreg, f, block_xyz, acc, false, uo);
-    }
-    e = e1;
-    js = js1;
-    e1 = e2;
-    js1 = js2;
-  }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-}
 
 template <int P, int THREADS, int MINB, bool MON>
 void launch_listed(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
-  if constexpr (!MON && HLBG_LIST_STAGE && P != 2) {
-    const int64_t warps = (a.n_warps + HLBG_LIST_UNITS - 1) / HLBG_LIST_UNITS;
-    const int64_t g = (warps * 32 + THREADS - 1) / THREADS;
-    if (g) k_stream_collide_listed_staged<P, THREADS, MINB, HLBG_LIST_UNITS><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
-    return;
-  }
-  if constexpr (!MON && HLBG_LIST_UNITS > 1) {
-    const int64_t warps = (a.n_warps + HLBG_LIST_UNITS - 1) / HLBG_LIST_UNITS;
-    const int64_t g = (warps * 32 + THREADS - 1) / THREADS;
-    if (g) k_stream_collide_listed_multi<P, THREADS, MINB, HLBG_LIST_UNITS><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
-    return;
-  }
   const int64_t g = (a.n_warps * 32 + THREADS - 1) / THREADS;
   if (g) k_stream_collide_listed<P, THREADS, MINB, MON><<<(unsigned)g, THREADS, 0, st>>>(a, bxyz);
 }
