@@ -315,9 +315,6 @@ __device__ __forceinline__ float weight_f(int i) {
   return i == 0 ? (float)(1.0 / 3.0) : (i < 7 ? (float)(1.0 / 18.0) : (float)(1.0 / 36.0));
 }
 
-#ifndef HLBG_RCP
-#define HLBG_RCP 0
-#endif
 __device__ __forceinline__ void moments_dev(const float* g, float& dr, float& mx, float& my,
                                             float& mz) {
   // pairwise grouping by direction families keeps FP32 rounding small
@@ -343,13 +340,7 @@ __device__ __forceinline__ void collide_dev(const StepArgs& a, const float* g, f
                                             float& my, float& mz, float* gpost, float wp_in,
                                             float wm_in) {
   moments_dev(g, dr, mx, my, mz);
-#if HLBG_RCP == 1
-  const float inv_rho = __frcp_rn(1.f + dr);  // the correctly rounded reciprocal, as 1.f / x
-#elif HLBG_RCP == 2
-  const float inv_rho = __fdividef(1.f, 1.f + dr);
-#else
   const float inv_rho = 1.f / (1.f + dr);
-#endif
   const float A = dr - 1.5f * (mx * mx + my * my + mz * mz) * inv_rho;
   const float c45 = 4.5f * inv_rho;
   const float wp = wp_in;

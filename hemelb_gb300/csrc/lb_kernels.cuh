@@ -198,65 +198,6 @@ struct PushAll<P, Q> {
   static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, int, int, int, const T*) {}
 };
 
-// HLBG_PUSH_PRECOMP=1: the bulk pushes take each axis's wrapped neighbour
-// coordinates and neighbour-table offsets from values computed once per site
-// (default layout only: identity in-block order, no packed blocks).
-#ifndef HLBG_PUSH_PRECOMP
-#define HLBG_PUSH_PRECOMP 0
-#endif
-struct PushGeo {
-  int tx_m, tx_0, tx_p, ty_m, ty_0, ty_p, tz_m, tz_0, tz_p;  // slot bits of x-1, x, x+1 (wrapped), ...
-  int kx_m, kx_p, ky_m, ky_p, kz_m, kz_p;                       // table-index steps at block faces
-  __device__ __forceinline__ PushGeo(int x, int y, int z) {
-    tx_0 = x << 6;
-    tx_m = ((x - 1) & 7) << 6;
-    tx_p = ((x + 1) & 7) << 6;
-    ty_0 = y << 3;
-    ty_m = ((y - 1) & 7) << 3;
-    ty_p = ((y + 1) & 7) << 3;
-    tz_0 = z;
-    tz_m = (z - 1) & 7;
-    tz_p = (z + 1) & 7;
-    kx_m = x == 0 ? -9 : 0;
-    kx_p = x == 7 ? 9 : 0;
-    ky_m = y == 0 ? -3 : 0;
-    ky_p = y == 7 ? 3 : 0;
-    kz_m = z == 0 ? -1 : 0;
-    kz_p = z == 7 ? 1 : 0;
-  }
-  template <int C>
-  __device__ __forceinline__ int tx() const { return C < 0 ? tx_m : (C > 0 ? tx_p : tx_0); }
-  template <int C>
-  __device__ __forceinline__ int ty() const { return C < 0 ? ty_m : (C > 0 ? ty_p : ty_0); }
-  template <int C>
-  __device__ __forceinline__ int tz() const { return C < 0 ? tz_m : (C > 0 ? tz_p : tz_0); }
-  template <int C>
-  __device__ __forceinline__ int kx() const { return C < 0 ? kx_m : (C > 0 ? kx_p : 0); }
-  template <int C>
-  __device__ __forceinline__ int ky() const { return C < 0 ? ky_m : (C > 0 ? ky_p : 0); }
-  template <int C>
-  __device__ __forceinline__ int kz() const { return C < 0 ? kz_m : (C > 0 ? kz_p : 0); }
-};
-
-template <int P, int D>
-struct PushBulkG {
-  template <class S, class T, class B>
-  static __device__ __forceinline__ void run(S* fn, const StepArgs& a, const B& base, const PushGeo& g,
-                                             bool store, const T* fpost) {
-    constexpr int cx = Lat::cx(D), cy = Lat::cy(D), cz = Lat::cz(D);
-    const int k = 13 + g.kx<cx>() + g.ky<cy>() + g.kz<cz>();
-    const int tl = g.tx<cx>() | g.ty<cy>() | g.tz<cz>();
-    const int32_t e = base(k);  // every lane shuffles
-    if (store) Store<P>::store(fn, (int64_t)e * (Q * kSites) + (D * kSites + tl), fpost[D], a);
-    PushBulkG<P, D + 1>::run(fn, a, base, g, store, fpost);
-  }
-};
-template <int P>
-struct PushBulkG<P, Q> {
-  template <class S, class T, class B>
-  static __device__ __forceinline__ void run(S*, const StepArgs&, const B&, const PushGeo&, bool, const T*) {}
-};
-
 // Pushes of the all-slots kernel: every lane takes part in the shuffles, only
 // bulk sites store.
 template <int P, int D>
@@ -669,11 +610,7 @@ __device__ __forceinline__ void collide_and_push(const StepArgs& a, int64_t b, i
   const int x = l >> 6, y = (l >> 3) & 7, z = l & 7;
   const bool bnd = code >= 2;
   if (__ballot_sync(0xffffffffu, bnd) == 0) {
-#if HLBG_PUSH_PRECOMP && !HLBG_PACK && !HLBG_BLOCK_ORDER
-    PushBulkG<P, 0>::run(fn, a, ShflBase{tabreg}, PushGeo(x, y, z), code == 1, fpost);
-#else
     PushBulk<P, 0>::run(fn, a, ShflBase{tabreg}, x, y, z, code == 1, fpost);
-#endif
   } else {
     const int64_t r = bnd ? (int64_t)code - 2 : 0;
     const uint64_t links = bnd ? a.b_links[r] : 0ull;

@@ -40,8 +40,19 @@ def _ok(rc, what):
         raise RuntimeError(f"{what} failed with status {rc}")
 
 
-def conv3d(x, w, bias, out, out_f32=None, taps=27, relu=False):
-    """out[n,z,y,x,co] = act(sum_{tap,ci} x[n,(z,y,x)+off(tap),ci] w[tap,co,ci] + bias[co])."""
+def tc_eligible(cin: int, cout: int, *tensors) -> bool:
+    """Shapes the tcgen05 convolution takes: C_in a multiple of 16, C_out a multiple
+    of 16 up to 256, 16-byte aligned buffers."""
+    return (cin % 16 == 0 and cout % 16 == 0 and 16 <= cout <= 256
+            and all(t is None or t.data_ptr() % 16 == 0 for t in tensors))
+
+
+def conv3d(x, w, bias, out, out_f32=None, taps=27, relu=False, engine="auto"):
+    """out[n,z,y,x,co] = act(sum_{tap,ci} x[n,(z,y,x)+off(tap),ci] w[tap,co,ci] + bias[co]).
+
+    engine "tc": the tcgen05 / TMEM / TMA kernel (hlbg_nn_conv3d_tc); "mma": the
+    mma.sync kernel (hlbg_nn_conv3d, every shape); "auto": tcgen05 where it takes
+    the shape, else mma.sync."""
     _need(x, _BF16, "conv3d input")
     _need(w, _BF16, "conv3d weights")
     _need(out, _BF16, "conv3d output")
@@ -53,25 +64,16 @@ def conv3d(x, w, bias, out, out_f32=None, taps=27, relu=False):
         _need(bias, _F32, "conv3d bias")
     if out_f32 is not None:
         _need(out_f32, _F32, "conv3d FP32 output")
-    _ok(_lib().hlbg_nn_conv3d(_p(x), cin, _p(w), _p(bias), _p(out), _p(out_f32), cout, n, d, h, wd,
-                              taps, int(relu), _stream()), "hlbg_nn_conv3d")
+    if engine == "auto":
+        engine = "tc" if tc_eligible(cin, cout, x, w, out, out_f32) else "mma"
+    fn = _lib().hlbg_nn_conv3d_tc if engine == "tc" else _lib().hlbg_nn_conv3d
+    _ok(fn(_p(x), cin, _p(w), _p(bias), _p(out), _p(out_f32), cout, n, d, h, wd, taps, int(relu), _stream()),
+        "hlbg_nn_conv3d_tc" if engine == "tc" else "hlbg_nn_conv3d")
 
 
 def conv3d_tc(x, w, bias, out, out_f32=None, taps=27, relu=False):
     """conv3d on the tcgen05 tensor cores (cin and cout multiples of 16, cout <= 256)."""
-    _need(x, _BF16, "conv3d input")
-    _need(w, _BF16, "conv3d weights")
-    _need(out, _BF16, "conv3d output")
-    n, d, h, wd, cin = x.shape
-    t, cout, cin_w = w.shape
-    if t != taps or cin_w != cin or out.shape != (n, d, h, wd, cout):
-        raise ValueError(f"conv3d shapes: x {tuple(x.shape)} w {tuple(w.shape)} out {tuple(out.shape)}")
-    if bias is not None:
-        _need(bias, _F32, "conv3d bias")
-    if out_f32 is not None:
-        _need(out_f32, _F32, "conv3d FP32 output")
-    _ok(_lib().hlbg_nn_conv3d_tc(_p(x), cin, _p(w), _p(bias), _p(out), _p(out_f32), cout, n, d, h, wd,
-                                 taps, int(relu), _stream()), "hlbg_nn_conv3d_tc")
+    conv3d(x, w, bias, out, out_f32, taps, relu, engine="tc")
 
 
 def tc_error(reset: bool = True) -> int:
@@ -88,13 +90,13 @@ def flip_transpose(w, wt):
     _ok(_lib().hlbg_nn_flip_transpose(_p(w), _p(wt), cout, cin, taps, _stream()), "hlbg_nn_flip_transpose")
 
 
-def conv3d_data_grad(dy, w, dx, dx_f32=None, wt=None):
+def conv3d_data_grad(dy, w, dx, dx_f32=None, wt=None, engine="auto"):
     """dx = conv(dy, flipped transposed w): the input gradient of conv3d."""
     taps, cout, cin = w.shape
     if wt is None:
         wt = torch.empty((taps, cin, cout), dtype=_BF16, device=w.device)
     flip_transpose(w, wt)
-    conv3d(dy, wt, None, dx, dx_f32, taps=taps, relu=False)
+    conv3d(dy, wt, None, dx, dx_f32, taps=taps, relu=False, engine=engine)
 
 
 def conv3d_weight_grad(x, dy, dw):

@@ -33,7 +33,7 @@ def test_conv_forward(cin, cout, taps, relu, shape):
     b = rng.standard_normal(cout).astype(np.float32)
     y = torch.empty(shape + (cout,), dtype=torch.bfloat16, device="cuda")
     y32 = torch.empty(shape + (cout,), dtype=torch.float32, device="cuda")
-    nn.conv3d(xt, wt, torch.tensor(b, device="cuda"), y, y32, taps=taps, relu=relu)
+    nn.conv3d(xt, wt, torch.tensor(b, device="cuda"), y, y32, taps=taps, relu=relu, engine="mma")
     torch.cuda.synchronize()
     ref = O.conv3d(x, w, b.astype(np.float64), relu=relu)
     # FP32 accumulation of exact BF16 products: tolerance 1e-4 of the output scale
@@ -65,21 +65,22 @@ def test_conv_forward_tcgen05(cin, cout, taps, relu, shape):
     assert close(y32.cpu().numpy(), ref, 1e-4)
     assert np.all(np.abs(y.float().cpu().numpy() - y32.cpu().numpy()) <= 2.0 ** -8 * np.abs(y32.cpu().numpy()) + 1e-30)
     z32 = torch.empty_like(y32)
-    nn.conv3d(xt, wt, bt, torch.empty_like(y), z32, taps=taps, relu=relu)
+    nn.conv3d(xt, wt, bt, torch.empty_like(y), z32, taps=taps, relu=relu, engine="mma")
     torch.cuda.synchronize()
     assert close(y32.cpu().numpy(), z32.cpu().numpy(), 1e-5)
 
 
 @pytest.mark.parametrize("cin,cout,shape", [(16, 32, (2, 6, 5, 4)), (32, 16, (2, 6, 5, 4)), (48, 48, (2, 6, 5, 4)),
                                              (32, 32, (2, 13, 20, 24)), (16, 48, (1, 9, 12, 17))])
-def test_conv_gradients(cin, cout, shape):
+@pytest.mark.parametrize("engine", ["mma", "auto"])
+def test_conv_gradients(cin, cout, shape, engine):
     rng = np.random.default_rng(7 + cin)
     x, xt = bf16(rng.standard_normal(shape + (cin,)))
     w, wt = bf16(rng.standard_normal((27, cout, cin)) / np.sqrt(27 * cin))
     dy, dyt = bf16(rng.standard_normal(shape + (cout,)))
     dx = torch.empty(shape + (cin,), dtype=torch.bfloat16, device="cuda")
     dx32 = torch.empty(shape + (cin,), dtype=torch.float32, device="cuda")
-    nn.conv3d_data_grad(dyt, wt, dx, dx32)
+    nn.conv3d_data_grad(dyt, wt, dx, dx32, engine=engine)
     dw = torch.zeros((27, cout, cin), dtype=torch.float32, device="cuda")
     nn.conv3d_weight_grad(xt, dyt, dw)
     db = torch.zeros(cout, dtype=torch.float32, device="cuda")
