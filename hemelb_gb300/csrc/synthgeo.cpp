@@ -365,7 +365,9 @@ struct Voxelizer {
           int ioid = -1;
           bool had_in = false, had_out = false;
           float cutv[26];
+          int hitv[26];
           for (int d = 1; d <= nl; ++d) cutv[d - 1] = -1.0f;  // NO_VALUE-like for fluid links
+          for (int d = 1; d <= nl; ++d) hitv[d - 1] = -1;
           Vec p{o[0] + i, o[1] + j, o[2] + k};
           for (int d = 1; d <= nl; ++d) {
             if (fl[i + 1 + cx[d]][j + 1 + cy[d]][k + 1 + cz[d]]) continue;
@@ -377,6 +379,7 @@ struct Voxelizer {
                 hit = ii;
                 break;
               }
+            hitv[d - 1] = hit;
             if (hit >= 0) {
               const Iolet& io = iolet_by(hit);
               im |= 1u << (d - 1);
@@ -398,6 +401,24 @@ struct Voxelizer {
                 cutv[d - 1] = (float)qv;
               }
             }
+          }
+          if (had_in && had_out) {
+            // A site with links to an inlet and to an outlet (an outlet plane that
+            // ends next to an inlet): SiteData holds one iolet id for a site typed
+            // INLET, so its outlet links become wall links (cut at the link's end).
+            ioid = -1;
+            for (int d = 1; d <= nl; ++d) {
+              if (!((im >> (d - 1)) & 1u)) continue;
+              const Iolet& io = iolet_by(hitv[d - 1]);
+              if (io.outlet) {
+                im &= ~(1u << (d - 1));
+                wm |= 1u << (d - 1);
+                cutv[d - 1] = 1.0f;
+              } else {
+                ioid = io.index;
+              }
+            }
+            had_out = false;
           }
           if (wm == 0 && im == 0) continue;
           // wall normal: gradient of the shape the site lies deepest in; else the
