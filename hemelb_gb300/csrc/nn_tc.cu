@@ -1,21 +1,27 @@
 // 3x3x3 convolution of the warm-start surrogate on the fifth-generation tensor
-// cores: tcgen05.mma with the accumulator in tensor memory (TMEM), operands staged
+// cores: tcgen05.mma with the accumulators in tensor memory (TMEM), operands staged
 // in shared memory by TMA (cp.async.bulk.tensor), completion tracked on mbarriers.
 //
-// Implicit GEMM.  One CTA computes one output brick of 8 (x) x 4 (y) x 4 (z) = 128
-// voxels -- the MMA's M = 128 rows -- for all C_out output channels (N = C_out,
-// a multiple of 16 up to 256).  The reduction runs over the 27 taps x C_in input
-// channels in steps of K = 16: for tap (dz, dy, dx) and channel slice k, a TMA
-// load copies the input brick shifted by (dx, dy, dz), channels [16k, 16k + 16),
-// as 128 rows of 32 bytes (coordinates outside the volume read zeros: that is the
-// convolution's zero padding), and a second TMA load copies the weights of that
-// tap and slice, C_out rows of 32 bytes.  Both land in the 32-byte-swizzled K-major
-// layout that the MMA's shared-memory descriptors name.  A ring of kStages such
-// stages keeps the copies ahead of the MMAs: one thread issues the copies (waiting
-// for a stage to be free), one thread issues the MMAs (waiting for a stage to be
-// full) and returns each stage with tcgen05.commit.  The four warps then read the
-// accumulator from TMEM (warp w owns TMEM lanes 32w..32w+31, i.e. 32 voxels), add
-// the bias, apply the ReLU and store BF16 (and optionally FP32) channels-last.
+// Implicit GEMM.  One CTA computes an output tile of 8 (x) x 16 (y) x BZ (z)
+// voxels for all C_out output channels: BZ MMAs of M = 128 rows (one z-plane each,
+// N = C_out, a multiple of 16 up to 256), each with its FP32 accumulator in its
+// own TMEM columns.  The reduction runs over C_in in slices of 16 channels and,
+// within a slice, over the 27 taps (K = 16 per MMA):
+//  * per slice, one TMA load brings the input tile with its halo -- 10 x 18 x 4
+//    voxels, 16 channels, in two planes of 8 channels (16-byte rows), positions
+//    outside the volume read as zeros, which is the convolution's zero padding --
+//    and every tap's A operand is a shared-memory descriptor into that one tile:
+//    the core-matrix layout without swizzle puts the 8 rows of a core matrix (8
+//    consecutive x) in 128 contiguous bytes and steps 160 bytes (one halo row of 10
+//    voxels) from one y to the next, so a tap is only a different start address;
+//  * per tap, a TMA load brings that tap's weights for the slice (C_out rows of 32
+//    bytes, in the 32-byte swizzle) into a ring of stages; every z-plane's MMA
+//    uses it (BZ = 2 z-planes per CTA, each accumulator C_out TMEM columns).
+// One thread issues the copies (waiting for a buffer to be free), one thread
+// issues the MMAs (waiting for it to be full) and returns each buffer with
+// tcgen05.commit.  The four warps then read the accumulators from TMEM (warp w
+// owns TMEM lanes 32w..32w+31: the rows y = 4w..4w+3 of the tile), add the bias,
+// apply the ReLU and store BF16 (and optionally FP32) channels-last.
 //
 // Every wait is bounded: a wait that gives up sets g_tc_err (read back by
 // hlbg_nn_tc_error), the CTA waits (bounded) for the copies it issued, frees its
@@ -26,16 +32,24 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/hemelb_gb300_nn.h"
 
 namespace {
 
-constexpr int kM = 128;                   // voxels per CTA: the MMA's M
-constexpr int kStages = 4;                // shared-memory ring depth
-constexpr int kASlice = kM * 32;          // one A stage: 128 rows x 16 BF16
-constexpr int64_t kWaitLimit = 1ll << 22; // polls before a wait gives up
+constexpr int kM = 128;                      // rows of one MMA: an 8 x 16 plane of voxels
+constexpr int kHX = 10, kHY = 18;            // input tile with its halo in x and y
+// z-planes per CTA (MMAs per weight stage): BZ; the input tile is BZ + 2 deep
+template <int BZ>
+struct Tile {
+  static constexpr int kHZ = BZ + 2;
+  static constexpr int kAPlane = kHX * kHY * kHZ * 16;  // bytes of 8 channels of the tile
+  static constexpr int kATile = 2 * kAPlane;            // one 16-channel slice
+};
+constexpr int kMaxBStages = 16;
+constexpr int64_t kWaitLimit = 1ll << 22;    // polls before a wait gives up
 
 __device__ int g_tc_err;
 
@@ -83,11 +97,24 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// Shared-memory matrix descriptor of a K-major tile of 32-byte rows in the
-// 32-byte swizzle: start address, leading-dimension offset (not used by swizzled
-// K-major tiles; 1 by convention), stride between 8-row groups (8 x 32 B), the
-// descriptor version of tcgen05 (1) and the layout code of the 32-byte swizzle (6).
-__device__ __forceinline__ uint64_t sw32_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor of a K-major operand in the core-matrix layout
+// without swizzle (core matrix: 8 rows x 16 bytes, contiguous): start address,
+// leading-dimension offset = bytes between the two core matrices along K (the two
+// 8-channel planes), stride-dimension offset = bytes between consecutive 8-row
+// groups, the descriptor version of tcgen05 (1) and layout code 0 (no swizzle).
+__device__ __forceinline__ uint64_t desc_noswizzle(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  return d;
+}
+
+// The same for a K-major tile of 32-byte rows (16 BF16) in the 32-byte swizzle
+// (the layout TMA writes with CU_TENSOR_MAP_SWIZZLE_32B): 8-row groups 256 bytes
+// apart, leading offset unused (1 by convention), layout code 6.
+__device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
   d |= (uint64_t)1u << 16;
@@ -129,23 +156,28 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
 struct TcParams {
   int Cin, Cout, N, D, H, W, taps, relu;
   int nbx, nby, nbz;
-  uint32_t ncols;        // TMEM columns allocated (a power of two >= 32 and >= Cout)
-  int b_stride;          // bytes of one B stage (C_out x 32, rounded up to 1024)
+  int b_stages;          // weight stages in the ring (<= kMaxBStages)
+  int b_stride;          // bytes of one weight stage (C_out x 32, rounded up to 128)
+  uint32_t ncols;        // TMEM columns allocated (a power of two >= 32 and >= 2 C_out)
   const float* bias;     // [C_out] or null
   __nv_bfloat16* out;    // [voxels][C_out]
   float* out_f32;        // [voxels][C_out] or null
 };
 
+template <int BZ>
 __global__ void __launch_bounds__(128, 1) k_conv3d_tc(const __grid_constant__ CUtensorMap tin,
                                                       const __grid_constant__ CUtensorMap tw, TcParams p) {
+  constexpr int kBZ = BZ, kAPlane = Tile<BZ>::kAPlane, kATile = Tile<BZ>::kATile;
+  constexpr int kARegion = (2 * kATile + 1023) / 1024 * 1024;  // the weight stages start 1024-aligned
   extern __shared__ uint8_t smem_raw[];
-  // stages at a 1024-byte boundary (TMA destinations and swizzle atoms)
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int stage_bytes = kASlice + p.b_stride;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + kStages * stage_bytes);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 1);
-  const uint32_t a0 = smem_u32(base), full0 = smem_u32(bars), empty0 = full0 + 8 * kStages,
-                 done = full0 + 16 * kStages;
+  // [input slice buffer 0 | buffer 1 | weight stages | barriers | TMEM address]
+  const uint32_t a_base = smem_u32(base);
+  const uint32_t b_base = a_base + kARegion;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + kARegion + p.b_stages * p.b_stride);
+  const uint32_t afull0 = smem_u32(bars), aempty0 = afull0 + 16, bfull0 = afull0 + 32,
+                 bempty0 = bfull0 + 8 * kMaxBStages, done = bempty0 + 8 * kMaxBStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 4 + 2 * kMaxBStages + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   int bid = blockIdx.x;
@@ -155,12 +187,16 @@ __global__ void __launch_bounds__(128, 1) k_conv3d_tc(const __grid_constant__ CU
   bid /= p.nby;
   const int bz = bid % p.nbz;
   const int n = bid / p.nbz;
-  const int x0 = bx * 8, y0 = by * 4, z0 = bz * 4;
+  const int x0 = bx * 8, y0 = by * 16, z0 = bz * kBZ;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, 1);
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(afull0 + 8 * s, 1);
+      mbar_init(aempty0 + 8 * s, 1);
+    }
+    for (int s = 0; s < p.b_stages; ++s) {
+      mbar_init(bfull0 + 8 * s, 1);
+      mbar_init(bempty0 + 8 * s, 1);
     }
     mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -177,89 +213,116 @@ __global__ void __launch_bounds__(128, 1) k_conv3d_tc(const __grid_constant__ CU
   const uint32_t tmem = *tmem_slot;
 
   const int kslices = p.Cin / 16;
-  const int ksteps = p.taps * kslices;
-  const uint32_t tx_bytes = (uint32_t)(kASlice + p.Cout * 32);
+  const int SB = p.b_stages;
+  const uint32_t b_bytes = (uint32_t)(p.Cout * 32);
   if (warp == 0 && lane == 0) {
-    // producer: the copies of k-step i go to stage i % kStages once it is free
-    int issued = 0;
+    // producer
+    int a_issued = 0, b_issued = 0;
     bool ok = true;
-    for (int i = 0; i < ksteps; ++i) {
-      const int s = i % kStages;
-      const uint32_t ph = (uint32_t)(i / kStages) & 1u;
-      if (!mbar_wait(empty0 + 8 * s, ph ^ 1u)) {
+    for (int ks = 0; ks < kslices && ok; ++ks) {
+      const int a = ks & 1;
+      if (!mbar_wait(aempty0 + 8 * a, ((uint32_t)(ks >> 1) & 1u) ^ 1u)) {
         ok = false;
         break;
       }
-      const int tap = i / kslices, ks = i % kslices;
-      int dz = 0, dy = 0, dx = 0;
-      if (p.taps == 27) {
-        dz = tap / 9 - 1;
-        dy = (tap / 3) % 3 - 1;
-        dx = tap % 3 - 1;
+      const uint32_t sa = a_base + a * kATile;
+      mbar_expect_tx(afull0 + 8 * a, (uint32_t)kATile);
+      tma_load_5d(sa, &tin, afull0 + 8 * a, ks * 16, x0 - 1, y0 - 1, z0 - 1, n);
+      tma_load_5d(sa + kAPlane, &tin, afull0 + 8 * a, ks * 16 + 8, x0 - 1, y0 - 1, z0 - 1, n);
+      ++a_issued;
+      for (int t = 0; t < p.taps; ++t) {
+        const int i = ks * p.taps + t, s = i % SB;
+        if (!mbar_wait(bempty0 + 8 * s, ((uint32_t)(i / SB) & 1u) ^ 1u)) {
+          ok = false;
+          break;
+        }
+        const uint32_t sb = b_base + s * p.b_stride;
+        mbar_expect_tx(bfull0 + 8 * s, b_bytes);
+        tma_load_3d(sb, &tw, bfull0 + 8 * s, ks * 16, 0, t);
+        ++b_issued;
       }
-      const uint32_t sa = a0 + s * stage_bytes;
-      mbar_expect_tx(full0 + 8 * s, tx_bytes);
-      tma_load_5d(sa, &tin, full0 + 8 * s, ks * 16, x0 + dx, y0 + dy, z0 + dz, n);
-      tma_load_3d(sa + kASlice, &tw, full0 + 8 * s, ks * 16, 0, tap);
-      ++issued;
     }
     if (!ok) {
       atomicExch(&g_tc_err, 1);
       // the copies in flight land before the CTA's shared memory goes away
-      for (int j = issued > kStages ? issued - kStages : 0; j < issued; ++j)
-        mbar_wait(full0 + 8 * (j % kStages), (uint32_t)(j / kStages) & 1u);
+      for (int j = a_issued > 2 ? a_issued - 2 : 0; j < a_issued; ++j)
+        mbar_wait(afull0 + 8 * (j & 1), (uint32_t)(j >> 1) & 1u);
+      for (int j = b_issued > SB ? b_issued - SB : 0; j < b_issued; ++j)
+        mbar_wait(bfull0 + 8 * (j % SB), (uint32_t)(j / SB) & 1u);
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer: k-step i once its stage is full; the commit returns the stage
+    // MMA issuer
     const uint32_t idesc = idesc_bf16(p.Cout);
-    for (int i = 0; i < ksteps; ++i) {
-      const int s = i % kStages;
-      const uint32_t ph = (uint32_t)(i / kStages) & 1u;
-      if (!mbar_wait(full0 + 8 * s, ph)) {
-        atomicExch(&g_tc_err, 1);
+    bool ok = true;
+    for (int ks = 0; ks < kslices && ok; ++ks) {
+      const int a = ks & 1;
+      if (!mbar_wait(afull0 + 8 * a, (uint32_t)(ks >> 1) & 1u)) {
+        ok = false;
         break;
       }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa = a0 + s * stage_bytes;
-      umma_bf16(tmem, sw32_desc(sa), sw32_desc(sa + kASlice), idesc, i > 0 ? 1u : 0u);
-      umma_commit(empty0 + 8 * s);
+      const uint32_t sa = a_base + a * kATile;
+      for (int t = 0; t < p.taps; ++t) {
+        const int i = ks * p.taps + t, s = i % SB;
+        if (!mbar_wait(bfull0 + 8 * s, (uint32_t)(i / SB) & 1u)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // the tap's offset in the halo tile (a 1x1x1 convolution uses the centre)
+        const int dz = p.taps == 27 ? t / 9 : 1, dy = p.taps == 27 ? (t / 3) % 3 : 1,
+                  dx = p.taps == 27 ? t % 3 : 1;
+        const uint64_t bdesc = desc_sw32(b_base + s * p.b_stride);
+#pragma unroll
+        for (int pz = 0; pz < kBZ; ++pz) {
+          const uint32_t start = sa + (uint32_t)((((pz + dz) * kHY + dy) * kHX + dx) * 16);
+          umma_bf16(tmem + (uint32_t)(pz * p.Cout), desc_noswizzle(start, (uint32_t)kAPlane, 160u), bdesc, idesc,
+                    (ks | t) != 0 ? 1u : 0u);
+        }
+        umma_commit(bempty0 + 8 * s);
+      }
+      umma_commit(aempty0 + 8 * a);
     }
+    if (!ok) atomicExch(&g_tc_err, 1);
     umma_commit(done);  // arrives once every MMA issued above has completed
   }
   __syncwarp();
 
-  // epilogue: TMEM lane = voxel row of the brick, column = output channel
+  // epilogue: TMEM lane = voxel row of a plane (x = row % 8, y = row / 8), columns
+  // [pz C_out, (pz + 1) C_out) = the output channels of z-plane pz
   const bool finished = mbar_wait(done, 0);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (!finished && lane == 0) atomicExch(&g_tc_err, 1);
   const int row = warp * 32 + lane;
-  const int x = x0 + (row & 7), y = y0 + ((row >> 3) & 3), z = z0 + (row >> 5);
-  const bool inside = finished && x < p.W && y < p.H && z < p.D;
-  const int64_t vox = (((int64_t)n * p.D + z) * p.H + y) * p.W + x;
-  for (int c0 = 0; c0 < p.Cout; c0 += 16) {
-    uint32_t r[16];
-    __syncwarp();  // tcgen05.ld is warp-collective: every lane, converged
-    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-    if (!inside) continue;
-    float v[16];
+  const int x = x0 + (row & 7), y = y0 + (row >> 3);
+  for (int pz = 0; pz < kBZ; ++pz) {
+    const int z = z0 + pz;
+    const bool inside = finished && x < p.W && y < p.H && z < p.D;
+    const int64_t vox = (((int64_t)n * p.D + z) * p.H + y) * p.W + x;
+    for (int c0 = 0; c0 < p.Cout; c0 += 16) {
+      uint32_t r[16];
+      __syncwarp();  // tcgen05.ld is warp-collective: every lane, converged
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(pz * p.Cout + c0), r);
+      if (!inside) continue;
+      float v[16];
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      v[j] = __uint_as_float(r[j]) + (p.bias ? __ldg(p.bias + c0 + j) : 0.f);
-      if (p.relu) v[j] = fmaxf(v[j], 0.f);
-    }
-    uint32_t packed[8];
+      for (int j = 0; j < 16; ++j) {
+        v[j] = __uint_as_float(r[j]) + (p.bias ? __ldg(p.bias + c0 + j) : 0.f);
+        if (p.relu) v[j] = fmaxf(v[j], 0.f);
+      }
+      uint32_t packed[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-      packed[j] = *reinterpret_cast<const uint32_t*>(&h);
-    }
-    uint4* dst = reinterpret_cast<uint4*>(p.out + vox * p.Cout + c0);
-    dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-    dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-    if (p.out_f32) {
-      float4* df = reinterpret_cast<float4*>(p.out_f32 + vox * p.Cout + c0);
+      for (int j = 0; j < 8; ++j) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        packed[j] = *reinterpret_cast<const uint32_t*>(&h);
+      }
+      uint4* dst = reinterpret_cast<uint4*>(p.out + vox * p.Cout + c0);
+      dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+      dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+      if (p.out_f32) {
+        float4* df = reinterpret_cast<float4*>(p.out_f32 + vox * p.Cout + c0);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) df[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        for (int j = 0; j < 4; ++j) df[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -298,15 +361,18 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
     return 1;
   auto enc = encode_fn();
   if (!enc) return 3;
+  // z-planes per CTA.  Four planes per weight stage (C_out <= 128) measured slower
+  // than two on the network's shapes (fewer CTAs per SM), so two throughout.
+  const int bz = 2;
   CUtensorMap tin, tw;
   {
     const cuuint64_t dims[5] = {(cuuint64_t)cin, (cuuint64_t)wd, (cuuint64_t)h, (cuuint64_t)d, (cuuint64_t)n};
     const cuuint64_t strides[4] = {(cuuint64_t)cin * 2, (cuuint64_t)cin * 2 * wd, (cuuint64_t)cin * 2 * wd * h,
                                    (cuuint64_t)cin * 2 * wd * h * d};
-    const cuuint32_t box[5] = {16, 8, 4, 4, 1};
+    const cuuint32_t box[5] = {8, (cuuint32_t)kHX, (cuuint32_t)kHY, (cuuint32_t)(bz + 2), 1};
     const cuuint32_t es[5] = {1, 1, 1, 1, 1};
     if (enc(&tin, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(in), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return 3;
   }
@@ -330,33 +396,39 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   p.taps = taps;
   p.relu = relu;
   p.nbx = (wd + 7) / 8;
-  p.nby = (h + 3) / 4;
-  p.nbz = (d + 3) / 4;
+  p.nby = (h + 15) / 16;
+  p.nbz = (d + bz - 1) / bz;
   uint32_t cols = 32;
-  while (cols < (uint32_t)cout) cols *= 2;
+  while (cols < (uint32_t)(bz * cout)) cols *= 2;
   p.ncols = cols;
-  p.b_stride = (cout * 32 + 1023) / 1024 * 1024;
+  p.b_stride = (cout * 32 + 1023) / 1024 * 1024;  // swizzled TMA destinations: 1024-byte aligned
   p.bias = bias;
   p.out = static_cast<__nv_bfloat16*>(out);
   p.out_f32 = out_f32;
-  // shared memory: the stages, the barriers and the TMEM address, plus alignment
-  // slack; at least enough that no more CTAs share an SM than its 512 TMEM
-  // columns can hold at once (an allocation beyond them would wait)
-  const int stage_bytes = kASlice + p.b_stride;
-  int smem = 1024 + kStages * stage_bytes + (2 * kStages + 1) * 8 + 16;
-  const int per_sm = 512 / (int)cols;
-  const int floor_bytes = 232448 / per_sm - 1024;
-  if (smem < floor_bytes && per_sm <= 8) smem = floor_bytes;
-  if (smem > 232448) return 1;
-  static thread_local int configured = 0;
-  if (configured < smem) {
-    if (cudaFuncSetAttribute(k_conv3d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess)
+  // CTAs per SM: at most what its 512 TMEM columns hold (an allocation beyond them
+  // would wait), at most 4 (2 with 4-plane tiles); each gets an equal share of the
+  // SM's shared memory, which is also its floor (so no more CTAs fit), and fills
+  // it with weight stages
+  const int a_tile = bz == 4 ? Tile<4>::kATile : Tile<2>::kATile;
+  const int per_sm = std::min(512 / (int)cols, bz == 4 ? 2 : 4);
+  const int share = 233472 / per_sm - 1024;  // per-SM capacity less the per-CTA reserve
+  const int fixed = 1024 + (2 * a_tile + 1023) / 1024 * 1024 + (4 + 2 * kMaxBStages + 1) * 8 + 16;
+  p.b_stages = std::min(kMaxBStages, (share - fixed) / p.b_stride);
+  if (p.b_stages < 2) return 1;
+  const int smem = std::min(share, 232448);
+  static thread_local bool configured = false;
+  if (!configured) {
+    if (cudaFuncSetAttribute(k_conv3d_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess ||
+        cudaFuncSetAttribute(k_conv3d_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess)
       return 3;
-    configured = 232448;
+    configured = true;
   }
   const int64_t grid = (int64_t)n * p.nbz * p.nby * p.nbx;
   if (grid > 0x7fffffff) return 1;
-  k_conv3d_tc<<<(unsigned)grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(tin, tw, p);
+  if (bz == 4)
+    k_conv3d_tc<4><<<(unsigned)grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(tin, tw, p);
+  else
+    k_conv3d_tc<2><<<(unsigned)grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(tin, tw, p);
   return cudaGetLastError() == cudaSuccess ? 0 : 3;
 }
 

@@ -47,6 +47,15 @@ def tc_eligible(cin: int, cout: int, *tensors) -> bool:
             and all(t is None or t.data_ptr() % 16 == 0 for t in tensors))
 
 
+def tc_tiles(n: int, d: int, h: int, w: int) -> int:
+    """CTAs of the tcgen05 convolution: one per 8 x 16 x 2 output tile."""
+    return n * -(-d // 2) * -(-h // 16) * -(-w // 8)
+
+
+# Below one tile per SM the mma.sync kernel is faster (measured on the 12^3 layers).
+_TC_MIN_TILES = 152
+
+
 def conv3d(x, w, bias, out, out_f32=None, taps=27, relu=False, engine="auto"):
     """out[n,z,y,x,co] = act(sum_{tap,ci} x[n,(z,y,x)+off(tap),ci] w[tap,co,ci] + bias[co]).
 
@@ -65,7 +74,8 @@ def conv3d(x, w, bias, out, out_f32=None, taps=27, relu=False, engine="auto"):
     if out_f32 is not None:
         _need(out_f32, _F32, "conv3d FP32 output")
     if engine == "auto":
-        engine = "tc" if tc_eligible(cin, cout, x, w, out, out_f32) else "mma"
+        engine = ("tc" if tc_eligible(cin, cout, x, w, out, out_f32) and tc_tiles(n, d, h, wd) >= _TC_MIN_TILES
+                  else "mma")
     fn = _lib().hlbg_nn_conv3d_tc if engine == "tc" else _lib().hlbg_nn_conv3d
     _ok(fn(_p(x), cin, _p(w), _p(bias), _p(out), _p(out_f32), cout, n, d, h, wd, taps, int(relu), _stream()),
         "hlbg_nn_conv3d_tc" if engine == "tc" else "hlbg_nn_conv3d")

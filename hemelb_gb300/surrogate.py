@@ -624,7 +624,8 @@ def bench_kernels(reps: int = 10, batch: int = 4):
         dw = torch.zeros((27, cout, cin), device="cuda")
         flop = 2.0 * 27 * cin * cout * batch * dim ** 3
         rec = {"voxels": batch * dim ** 3, "c_in": cin, "c_out": cout,
-               "tc_forward": nn.tc_eligible(cin, cout), "tc_input_grad": nn.tc_eligible(cout, cin)}
+               "tc_forward": nn.tc_eligible(cin, cout), "tc_input_grad": nn.tc_eligible(cout, cin),
+               "tc_tiles": nn.tc_tiles(batch, dim, dim, dim)}
         for name, fn in (("forward", lambda: nn.conv3d(x, w, b, y, None, 27, True, engine="mma")),
                          ("forward_tc", lambda: nn.conv3d(x, w, b, y, None, 27, True, engine="auto")),
                          ("input_grad", lambda: nn.conv3d_data_grad(y, w, dx, None, wt, engine="mma")),
