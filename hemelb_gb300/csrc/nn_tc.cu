@@ -14,9 +14,10 @@
 //    the core-matrix layout without swizzle puts the 8 rows of a core matrix (8
 //    consecutive x) in 128 contiguous bytes and steps 160 bytes (one halo row of 10
 //    voxels) from one y to the next, so a tap is only a different start address;
-//  * per tap, a TMA load brings that tap's weights for the slice (C_out rows of 32
-//    bytes, in the 32-byte swizzle) into a ring of stages; every z-plane's MMA
-//    uses it (BZ = 2 z-planes per CTA, each accumulator C_out TMEM columns).
+//  * per three taps (one x-row of the stencil), a TMA load brings their weights
+//    for the slice (3 x C_out rows of 32 bytes, in the 32-byte swizzle) into a
+//    ring of stages: six MMAs per stage -- three taps for each of BZ = 2 z-planes,
+//    each accumulator C_out TMEM columns.
 // One thread issues the copies (waiting for a buffer to be free), one thread
 // issues the MMAs (waiting for it to be full) and returns each buffer with
 // tcgen05.commit.  The four warps then read the accumulators from TMEM (warp w
@@ -157,6 +158,7 @@ struct TcParams {
   int Cin, Cout, N, D, H, W, taps, relu;
   int nbx, nby, nbz;
   int b_stages;          // weight stages in the ring (<= kMaxBStages)
+  int tps;               // taps per weight stage (3: one x-row of taps; 1 for a 1x1x1 convolution)
   int b_stride;          // bytes of one weight stage (C_out x 32, rounded up to 128)
   uint32_t ncols;        // TMEM columns allocated (a power of two >= 32 and >= 2 C_out)
   const float* bias;     // [C_out] or null
@@ -214,7 +216,8 @@ __global__ void __launch_bounds__(128, 1) k_conv3d_tc(const __grid_constant__ CU
 
   const int kslices = p.Cin / 16;
   const int SB = p.b_stages;
-  const uint32_t b_bytes = (uint32_t)(p.Cout * 32);
+  const int groups = p.taps / p.tps;  // weight stages per channel slice
+  const uint32_t b_bytes = (uint32_t)(p.tps * p.Cout * 32);
   if (warp == 0 && lane == 0) {
     // producer
     int a_issued = 0, b_issued = 0;
@@ -230,15 +233,15 @@ __global__ void __launch_bounds__(128, 1) k_conv3d_tc(const __grid_constant__ CU
       tma_load_5d(sa, &tin, afull0 + 8 * a, ks * 16, x0 - 1, y0 - 1, z0 - 1, n);
       tma_load_5d(sa + kAPlane, &tin, afull0 + 8 * a, ks * 16 + 8, x0 - 1, y0 - 1, z0 - 1, n);
       ++a_issued;
-      for (int t = 0; t < p.taps; ++t) {
-        const int i = ks * p.taps + t, s = i % SB;
+      for (int tg = 0; tg < groups; ++tg) {
+        const int i = ks * groups + tg, s = i % SB;
         if (!mbar_wait(bempty0 + 8 * s, ((uint32_t)(i / SB) & 1u) ^ 1u)) {
           ok = false;
           break;
         }
         const uint32_t sb = b_base + s * p.b_stride;
         mbar_expect_tx(bfull0 + 8 * s, b_bytes);
-        tma_load_3d(sb, &tw, bfull0 + 8 * s, ks * 16, 0, t);
+        tma_load_3d(sb, &tw, bfull0 + 8 * s, ks * 16, 0, tg * p.tps);
         ++b_issued;
       }
     }
@@ -261,22 +264,25 @@ __global__ void __launch_bounds__(128, 1) k_conv3d_tc(const __grid_constant__ CU
         break;
       }
       const uint32_t sa = a_base + a * kATile;
-      for (int t = 0; t < p.taps; ++t) {
-        const int i = ks * p.taps + t, s = i % SB;
+      for (int tg = 0; tg < groups; ++tg) {
+        const int i = ks * groups + tg, s = i % SB;
         if (!mbar_wait(bfull0 + 8 * s, (uint32_t)(i / SB) & 1u)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // the tap's offset in the halo tile (a 1x1x1 convolution uses the centre)
-        const int dz = p.taps == 27 ? t / 9 : 1, dy = p.taps == 27 ? (t / 3) % 3 : 1,
-                  dx = p.taps == 27 ? t % 3 : 1;
-        const uint64_t bdesc = desc_sw32(b_base + s * p.b_stride);
+        for (int j = 0; j < p.tps; ++j) {
+          const int t = tg * p.tps + j;
+          // the tap's offset in the halo tile (a 1x1x1 convolution uses the centre)
+          const int dz = p.taps == 27 ? t / 9 : 1, dy = p.taps == 27 ? (t / 3) % 3 : 1,
+                    dx = p.taps == 27 ? t % 3 : 1;
+          const uint64_t bdesc = desc_sw32(b_base + s * p.b_stride + (uint32_t)(j * p.Cout * 32));
 #pragma unroll
-        for (int pz = 0; pz < kBZ; ++pz) {
-          const uint32_t start = sa + (uint32_t)((((pz + dz) * kHY + dy) * kHX + dx) * 16);
-          umma_bf16(tmem + (uint32_t)(pz * p.Cout), desc_noswizzle(start, (uint32_t)kAPlane, 160u), bdesc, idesc,
-                    (ks | t) != 0 ? 1u : 0u);
+          for (int pz = 0; pz < kBZ; ++pz) {
+            const uint32_t start = sa + (uint32_t)((((pz + dz) * kHY + dy) * kHX + dx) * 16);
+            umma_bf16(tmem + (uint32_t)(pz * p.Cout), desc_noswizzle(start, (uint32_t)kAPlane, 160u), bdesc,
+                      idesc, (ks | t) != 0 ? 1u : 0u);
+          }
         }
         umma_commit(bempty0 + 8 * s);
       }
@@ -379,7 +385,7 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   {
     const cuuint64_t dims[3] = {(cuuint64_t)cin, (cuuint64_t)cout, (cuuint64_t)taps};
     const cuuint64_t strides[2] = {(cuuint64_t)cin * 2, (cuuint64_t)cin * 2 * cout};
-    const cuuint32_t box[3] = {16, (cuuint32_t)cout, 1};
+    const cuuint32_t box[3] = {16, (cuuint32_t)cout, (cuuint32_t)(taps == 27 ? 3 : 1)};
     const cuuint32_t es[3] = {1, 1, 1};
     if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(w), dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -401,7 +407,8 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   uint32_t cols = 32;
   while (cols < (uint32_t)(bz * cout)) cols *= 2;
   p.ncols = cols;
-  p.b_stride = (cout * 32 + 1023) / 1024 * 1024;  // swizzled TMA destinations: 1024-byte aligned
+  p.tps = taps == 27 ? 3 : 1;
+  p.b_stride = (p.tps * cout * 32 + 1023) / 1024 * 1024;  // swizzled TMA destinations: 1024-byte aligned
   p.bias = bias;
   p.out = static_cast<__nv_bfloat16*>(out);
   p.out_f32 = out_f32;
@@ -410,10 +417,14 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   // SM's shared memory, which is also its floor (so no more CTAs fit), and fills
   // it with weight stages
   const int a_tile = bz == 4 ? Tile<4>::kATile : Tile<2>::kATile;
-  const int per_sm = std::min(512 / (int)cols, bz == 4 ? 2 : 4);
-  const int share = 233472 / per_sm - 1024;  // per-SM capacity less the per-CTA reserve
   const int fixed = 1024 + (2 * a_tile + 1023) / 1024 * 1024 + (4 + 2 * kMaxBStages + 1) * 8 + 16;
-  p.b_stages = std::min(kMaxBStages, (share - fixed) / p.b_stride);
+  // fewer CTAs per SM when four weight stages would not fit in an equal share
+  int per_sm = std::min(512 / (int)cols, bz == 4 ? 2 : 4), share = 0;
+  for (;; --per_sm) {
+    share = 233472 / per_sm - 1024;  // per-SM capacity less the per-CTA reserve
+    p.b_stages = std::min(kMaxBStages, (std::min(share, 232448) - fixed) / p.b_stride);
+    if (p.b_stages >= 4 || per_sm == 1) break;
+  }
   if (p.b_stages < 2) return 1;
   const int smem = std::min(share, 232448);
   static thread_local bool configured = false;
