@@ -14,10 +14,11 @@
 //    the core-matrix layout without swizzle puts the 8 rows of a core matrix (8
 //    consecutive x) in 128 contiguous bytes and steps 160 bytes (one halo row of 10
 //    voxels) from one y to the next, so a tap is only a different start address;
-//  * per three taps (one x-row of the stencil), a TMA load brings their weights
-//    for the slice (3 x C_out rows of 32 bytes, in the 32-byte swizzle) into a
-//    ring of stages: six MMAs per stage -- three taps for each of BZ = 2 z-planes,
-//    each accumulator C_out TMEM columns.
+//  * per three taps (one x-row of the stencil; nine -- a z-plane of it -- when
+//    C_out > 128), a TMA load brings their weights for the slice (3 or 9 x C_out
+//    rows of 32 bytes, in the 32-byte swizzle) into a ring of stages: each tap
+//    feeds one MMA per z-plane (BZ = 2 z-planes, each accumulator C_out TMEM
+//    columns).
 // One thread issues the copies (waiting for a buffer to be free), one thread
 // issues the MMAs (waiting for it to be full) and returns each buffer with
 // tcgen05.commit.  The four warps then read the accumulators from TMEM (warp w
@@ -385,7 +386,7 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   {
     const cuuint64_t dims[3] = {(cuuint64_t)cin, (cuuint64_t)cout, (cuuint64_t)taps};
     const cuuint64_t strides[2] = {(cuuint64_t)cin * 2, (cuuint64_t)cin * 2 * cout};
-    const cuuint32_t box[3] = {16, (cuuint32_t)cout, (cuuint32_t)(taps == 27 ? 3 : 1)};
+    const cuuint32_t box[3] = {16, (cuuint32_t)cout, (cuuint32_t)(taps == 27 ? (2 * cout > 256 ? 9 : 3) : 1)};
     const cuuint32_t es[3] = {1, 1, 1};
     if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(w), dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -407,7 +408,10 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   uint32_t cols = 32;
   while (cols < (uint32_t)(bz * cout)) cols *= 2;
   p.ncols = cols;
-  p.tps = taps == 27 ? 3 : 1;
+  // taps per weight stage: one x-row of the stencil (3), or a whole z-plane of it (9)
+  // when 2 C_out > 256 TMEM columns leave the SM to one CTA anyway (measured: 9
+  // is faster there, 3 where two or more CTAs share an SM)
+  p.tps = taps == 27 ? (2 * cout > 256 ? 9 : 3) : 1;
   p.b_stride = (p.tps * cout * 32 + 1023) / 1024 * 1024;  // swizzled TMA destinations: 1024-byte aligned
   p.bias = bias;
   p.out = static_cast<__nv_bfloat16*>(out);
