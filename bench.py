@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--members", type=int, default=512)
+    ap.add_argument("--checkpoints", default="",
+                    help="tree_precision report: comma-separated steps at which to compare the forms")
     ap.add_argument("--report", default=None, choices=["precision", "steady", "ensemble", "tree_precision"],
                     help="print a report instead of the throughput line")
     return ap.parse_args()
@@ -289,9 +291,11 @@ def main():
         if args.report == "precision":
             print(json.dumps(reports.precision_report(steps=args.steps)), flush=True)
         elif args.report == "tree_precision":
+            cps = [int(c) for c in args.checkpoints.split(",") if c] or None
             print(json.dumps(reports.tree_precision_report(steps=args.steps, roots=args.roots,
                                                            box=args.box, depth=args.depth,
-                                                           root_radius=args.root_radius)), flush=True)
+                                                           root_radius=args.root_radius,
+                                                           checkpoints=cps)), flush=True)
         elif args.report == "ensemble":
             print(json.dumps(reports.ensemble_report(args.members, steps=args.steps,
                                                      warmup=args.warmup)), flush=True)
