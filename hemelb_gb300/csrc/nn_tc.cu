@@ -35,6 +35,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include "../../include/hemelb_gb300_nn.h"
@@ -417,13 +418,13 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   p.out = static_cast<__nv_bfloat16*>(out);
   p.out_f32 = out_f32;
   // CTAs per SM: at most what its 512 TMEM columns hold (an allocation beyond them
-  // would wait), at most 4 (2 with 4-plane tiles); each gets an equal share of the
+  // would wait), at most 4; each gets an equal share of the
   // SM's shared memory, which is also its floor (so no more CTAs fit), and fills
   // it with weight stages
-  const int a_tile = bz == 4 ? Tile<4>::kATile : Tile<2>::kATile;
+  const int a_tile = Tile<2>::kATile;
   const int fixed = 1024 + (2 * a_tile + 1023) / 1024 * 1024 + (4 + 2 * kMaxBStages + 1) * 8 + 16;
   // fewer CTAs per SM when four weight stages would not fit in an equal share
-  int per_sm = std::min(512 / (int)cols, bz == 4 ? 2 : 4), share = 0;
+  int per_sm = std::min(512 / (int)cols, 4), share = 0;
   for (;; --per_sm) {
     share = 233472 / per_sm - 1024;  // per-SM capacity less the per-CTA reserve
     p.b_stages = std::min(kMaxBStages, (std::min(share, 232448) - fixed) / p.b_stride);
@@ -431,19 +432,18 @@ int hlbg_nn_conv3d_tc(const void* in, int32_t cin, const void* w, const float* b
   }
   if (p.b_stages < 2) return 1;
   const int smem = std::min(share, 232448);
-  static thread_local bool configured = false;
-  if (!configured) {
-    if (cudaFuncSetAttribute(k_conv3d_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess ||
-        cudaFuncSetAttribute(k_conv3d_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess)
+  // the opt-in shared-memory limit is a per-device attribute of the kernel
+  static std::atomic<bool> configured[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 3;
+  if (!configured[dev].load()) {
+    if (cudaFuncSetAttribute(k_conv3d_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448) != cudaSuccess)
       return 3;
-    configured = true;
+    configured[dev].store(true);
   }
   const int64_t grid = (int64_t)n * p.nbz * p.nby * p.nbx;
   if (grid > 0x7fffffff) return 1;
-  if (bz == 4)
-    k_conv3d_tc<4><<<(unsigned)grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(tin, tw, p);
-  else
-    k_conv3d_tc<2><<<(unsigned)grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(tin, tw, p);
+  k_conv3d_tc<2><<<(unsigned)grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(tin, tw, p);
   return cudaGetLastError() == cudaSuccess ? 0 : 3;
 }
 
