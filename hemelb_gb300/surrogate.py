@@ -550,52 +550,73 @@ def summarise(evals) -> dict:
     return res
 
 
-def accuracy_study(net: UNet, samples, box: int, check_every: int = 50, log=None):
+def _field_at(grid, coords, smp: Sample, u_ref: float):
+    """(rho, u) in lattice units at the fluid sites `coords` from a predicted box
+    grid (B, B, B, 4) of normalised (u, p)."""
+    v = grid[coords[:, 0], coords[:, 1], coords[:, 2]].astype(np.float64)
+    return 1.0 + v[:, 3] * smp.drho, v[:, :3] * u_ref
+
+
+def _accuracy_one(i: int, smp: Sample, grid, check_every: int) -> dict:
+    g = smp.geometry()
+    ur = smp.u_ref(g)
+    runner = SteadyRunner(smp.case(g), ur)
+    s = runner.s
+    try:
+        rest, _, u_p = runner.run(timed=False)
+        steps_rest = rest["steps_run"]
+        s.RunToSteady(1e-9, ur, max(3 * steps_rest, 20000), runner.check_batch)
+        u_ref_field = s.macro()[1]
+        e_plain = rel_l2(u_p, u_ref_field)
+        rec = {"sample": i, "kind": smp.kind, "tau": smp.tau, "rest_steps": steps_rest,
+               "rest_error": e_plain}
+        for arm in ("rest_avg", "warm"):
+            if arm == "rest_avg":
+                s.SetInitialConditions()
+            else:
+                s.SetInitialField(*_field_at(grid, runner.coords, smp, ur))
+            s.DoTimeStep(1)
+            s.AverageTimeLevels()
+            steps, err = 1, float("inf")
+            while steps < 4 * steps_rest:
+                s.DoTimeStepGraph(check_every)
+                steps += check_every
+                err = rel_l2(s.macro()[1], u_ref_field)
+                if err <= e_plain:
+                    break
+            rec[arm + "_steps_to_match"] = steps if err <= e_plain else -1
+            rec[arm + "_error"] = err
+    finally:
+        runner.close()
+    return rec
+
+
+def accuracy_study(net: UNet, samples, box: int, check_every: int = 50, workers: int = 8, log=None):
     """Steps to the plain solve's own accuracy.  A reference field comes from the
     plain solve continued to max |du| / U_ref <= 1e-9 (or three times its steps);
     the plain solve's error against it is the accuracy to match.  The rest start
     with averaging and the warm start are then stepped, checked every
-    `check_every` steps, until their error against the reference is no larger."""
-    grids = Grids(len(samples), box, with_targets=False)
-    out = []
-    for i, smp in enumerate(samples):
-        g = smp.geometry()
-        grids.put(i, g, smp)
-        ur = smp.u_ref(g)
-        runner = SteadyRunner(smp.case(g), ur)
-        s = runner.s
-        try:
-            rest, _, u_p = runner.run()
-            steps_rest = rest["steps_run"]
-            s.RunToSteady(1e-9, ur, max(3 * steps_rest, 20000), runner.check_batch)
-            u_ref_field = s.macro()[1]
-            e_plain = rel_l2(u_p, u_ref_field)
-            rec = {"sample": i, "kind": smp.kind, "tau": smp.tau, "rest_steps": steps_rest,
-                   "rest_error": e_plain}
-            pred = lambda co: predict(net, grids, i, smp, co, ur)
-            for arm, start in (("rest_avg", None), ("warm", pred)):
-                if start is None:
-                    s.SetInitialConditions()
-                else:
-                    s.SetInitialField(*start(runner.coords))
-                s.DoTimeStep(1)
-                s.AverageTimeLevels()
-                steps, err = 1, float("inf")
-                while steps < 4 * steps_rest:
-                    s.DoTimeStepGraph(check_every)
-                    steps += check_every
-                    err = rel_l2(s.macro()[1], u_ref_field)
-                    if err <= e_plain:
-                        break
-                rec[arm + "_steps_to_match"] = steps if err <= e_plain else -1
-                rec[arm + "_error"] = err
-        finally:
-            runner.close()
-        out.append(rec)
-        if log and (i + 1) % 10 == 0:
-            log("accuracy study %d/%d" % (i + 1, len(samples)))
+    `check_every` steps, until their error against the reference is no larger.
+    The predictions are made first; the samples then run `workers` contexts at a
+    time (steps are counted, not timed)."""
+    from concurrent.futures import ThreadPoolExecutor
+    grids = Grids(1, box, with_targets=False)
+    preds = []
+    for smp in samples:
+        grids.put(0, smp.geometry(), smp)
+        preds.append(net.forward(grids.features([0]))[0][..., :4].float().cpu().numpy())
+    del grids
+    out = [None] * len(samples)
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        futs = [ex.submit(_accuracy_one, i, smp, preds[i], check_every) for i, smp in enumerate(samples)]
+        for i, f in enumerate(futs):
+            out[i] = f.result()
+            preds[i] = None
+            if log and (i + 1) % 25 == 0:
+                log("accuracy study %d/%d" % (i + 1, len(samples)))
     ok = [r for r in out if r["warm_steps_to_match"] > 0]
-    summ = {"n": len(out), "matched": len(ok),
+    both = [r for r in ok if r["rest_avg_steps_to_match"] > 0]
+    summ = {"n": len(out), "matched": len(ok), "rest_avg_matched": len(both),
             "median_rest_error": float(np.median([r["rest_error"] for r in out])),
             "rest_steps_total": float(sum(r["rest_steps"] for r in ok)),
             "warm_steps_to_match_total": float(sum(r["warm_steps_to_match"] for r in ok)),
@@ -604,6 +625,13 @@ def accuracy_study(net: UNet, samples, box: int, check_every: int = 50, log=None
         summ["speedup_at_same_accuracy_vs_rest"] = summ["rest_steps_total"] / summ["warm_steps_to_match_total"]
         summ["median_speedup_at_same_accuracy"] = float(np.median(
             [r["rest_steps"] / r["warm_steps_to_match"] for r in ok]))
+    if both:
+        # what the trained network adds over the same start without it (rest +
+        # one average), on the samples where both reach the plain solve's accuracy
+        summ["network_gain_at_same_accuracy"] = (sum(r["rest_avg_steps_to_match"] for r in both)
+                                                 / sum(r["warm_steps_to_match"] for r in both))
+        summ["median_network_gain_at_same_accuracy"] = float(np.median(
+            [r["rest_avg_steps_to_match"] / r["warm_steps_to_match"] for r in both]))
     return out, summ
 
 
@@ -656,7 +684,7 @@ def main(argv=None):
     ap.add_argument("--train-seconds", type=float, default=900.0)
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--plain-warm", type=int, default=16)
-    ap.add_argument("--accuracy-study", type=int, default=32)
+    ap.add_argument("--accuracy-study", type=int, default=300)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--out", default="")
     ap.add_argument("--save-weights", default="")
@@ -682,7 +710,7 @@ def main(argv=None):
     torch.cuda.empty_cache()
     evals = evaluate(net, test_s, a.box, plain_warm=a.plain_warm, log=log)
     summ = summarise(evals)
-    acc, acc_summ = accuracy_study(net, test_s[:a.accuracy_study], a.box, log=log)
+    acc, acc_summ = accuracy_study(net, test_s[:a.accuracy_study], a.box, workers=a.workers, log=log)
     doc = {"workload": "%d training + %d held-out seeded stenoses/bifurcations in a %d^3 box, D3Q19 LBGK "
                        "FP64, bounce-back walls, Nash pressure iolets" % (a.train, a.test, a.box),
            "criterion": "max |u_new - u_old| / U_ref <= 1e-6 after every step",
