@@ -636,16 +636,22 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
   ctx->n_ps = (int64_t)ctx->h_ps_slot.size();
   ctx->nb = nb;
   ctx->nslot = nslot;
-  // Packed builds (HLBG_PACK) pack every block that is not entirely fluid: its
-  // fluid sites take slots 0 .. nf-1 in site order and its solid sites the rest.
+  // Packed builds (HLBG_PACK) pack the partly fluid blocks whose fluid sites fill
+  // less than HLBG_PACK_FILL % of the z-rows they touch: their fluid sites take
+  // slots 0 .. nf-1 in site order and their solid sites the rest.
   // Everything above was built with slot = local site index; map it now (every
   // block: the in-block order of slot_in_block, packed blocks their own).
   std::vector<uint16_t> site2slot((size_t)nslot), slot2site((size_t)nslot);
   std::vector<uint8_t> packed((size_t)nb, 0);
   parallel_for(nb, [&](int64_t b) {
-    int nf = 0;
-    for (int w = 0; w < 8; ++w) nf += __builtin_popcountll(mask[b * 8 + w]);
-    packed[b] = HLBG_PACK && nf < 512;
+    int nf = 0, rows = 0;
+    for (int w = 0; w < 8; ++w) {
+      nf += __builtin_popcountll(mask[b * 8 + w]);
+      for (int k = 0; k < 8; ++k) rows += ((mask[b * 8 + w] >> (8 * k)) & 0xffull) != 0;
+    }
+    // only blocks whose fluid fills less than HLBG_PACK_FILL % of the z-rows
+    // (sectors) it touches
+    packed[b] = HLBG_PACK && nf < 512 && nf * 100 < HLBG_PACK_FILL * 8 * rows;
     if (!packed[b]) {  // the fixed in-block order of slot_in_block
       for (int l = 0; l < 512; ++l) {
         const int j = slot_of_local(l);

@@ -90,6 +90,9 @@ constexpr unsigned kListBoundary = 1u << 14;
 #ifndef HLBG_PACK
 #define HLBG_PACK 0
 #endif
+#ifndef HLBG_PACK_FILL
+#define HLBG_PACK_FILL 101
+#endif
 
 // Order of the 512 slots of a block.  HLBG_BLOCK_ORDER=0 (default): z-rows,
 // slot = (x*8 + y)*8 + z, so a 32-byte sector of FP32 values is a 1x1x8 row.  1:
