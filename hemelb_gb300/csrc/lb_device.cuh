@@ -85,8 +85,11 @@ constexpr int32_t kPackedBit = 1 << 30;
 // Flag of a fluid-list entry whose site has a boundary record (site_code >= 2).
 constexpr unsigned kListBoundary = 1u << 14;
 // HLBG_PACK=1 builds the packed layout (fluid sites of partly fluid blocks in the
-// first slots).  It moves 5-12% fewer bytes but the slot lookups of the pushes cost
-// more than that saves (measured on the vascular forest), so the default is off.
+// first slots; with HLBG_PACK_FILL=p only the blocks whose fluid fills less than
+// p % of the z-rows it touches).  It moves 5-12% fewer bytes but the packed code
+// path of the pushes (a flag test and a conditional slot lookup each) costs more
+// than that saves, whatever the share of packed blocks (measured on the vascular
+// forest), so the default is off.
 #ifndef HLBG_PACK
 #define HLBG_PACK 0
 #endif
