@@ -47,7 +47,7 @@ KERNEL_OF_VARIANT = {-1: "k_stream_collide<P, 128, 2>", 0: "k_stream_collide<P, 
                      1: "k_stream_collide<P, 128, 8>", 2: "k_stream_collide<P, 256, 4>",
                      3: "k_stream_collide<P, 512, 2>", 4: "k_stream_collide_block<P, 256, 4>",
                      5: "k_stream_collide_listed<P, 128, 9>", 6: "k_stream_collide_listed<P, 128, 8>",
-                     7: "k_stream_collide_listed<P, 64, 16>"}
+                     7: "k_stream_collide_listed<P, 64, 16>", 8: "k_stream_collide_pipe<P, 31, S>"}
 DTYPE = {0: "f64", 1: "f32", 2: "f16-storage/f32"}
 METRIC = "fluid MLUPS (D3Q19 LB update)"
 
@@ -345,6 +345,7 @@ def main():
             else "k_stream_collide<0, 128, 2>"
     else:
         kname = KERNEL_OF_VARIANT.get(variant, "k_stream_collide").replace("<P", "<%d" % prec)
+        kname = kname.replace(", S>", ", %d>" % (4 if prec == 1 else 8))
     base = kname.split("<")[0]
     # DRAM bytes per site from the ncu capture of one launch of this kernel on a small
     # case of the same generator (one tree in a 512^3 box, root radius 50, depth 6:

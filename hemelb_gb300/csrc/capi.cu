@@ -272,6 +272,7 @@ void fill_args(hlbg_ctx* ctx, StepArgs& a) {
   a.blk_runs = ctx->d_blk_runs;
   a.n_blocks = ctx->nb;
   a.stage_err = ctx->d_stage_err;
+  a.pipe_ctr = ctx->d_stage_err + 1;
   a.lane_slot = ctx->d_lane_slot;
   a.n_warps = ctx->n_warps;
   a.site_code = ctx->d_site_code;
@@ -776,8 +777,9 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
     if ((rc = upload(ctx, &ctx->d_blk_run_off, roff))) return rc;
     if ((rc = upload(ctx, &ctx->d_blk_runs, runs))) return rc;
   }
-  if ((rc = dev_alloc(ctx, &ctx->d_stage_err, 1))) return rc;
-  CK(cudaMemset(ctx->d_stage_err, 0, sizeof(int32_t)));
+  // [0]: the staged launches' error flag; [1]: the pipelined launch's block counter
+  if ((rc = dev_alloc(ctx, &ctx->d_stage_err, 2))) return rc;
+  CK(cudaMemset(ctx->d_stage_err, 0, 2 * sizeof(int32_t)));
   if ((rc = upload(ctx, &ctx->d_block_nbr, bnbr))) return rc;
   if (HLBG_PACK) {  // the kernels read the tables only in packed builds
     if ((rc = upload(ctx, &ctx->d_slot2site, slot2site))) return rc;
@@ -1013,11 +1015,11 @@ std::vector<IoletDev> iolet_table(const hlbg_ctx* ctx) {
   return iod;
 }
 
-// A block-staged CTA that gave up waiting for its staged rows leaves a flag.
+// A staged or pipelined CTA that gave up waiting for its staged rows leaves a flag.
 int check_stage_err(hlbg_ctx* ctx) {
   int32_t e = 0;
   CK(cudaMemcpy(&e, ctx->d_stage_err, sizeof(e), cudaMemcpyDeviceToHost));
-  if (e) return fail(ctx, HLBG_ERR_TIMEOUT, "a block-staged update gave up waiting for its copies");
+  if (e) return fail(ctx, HLBG_ERR_TIMEOUT, "a staged update gave up waiting for its copies");
   return HLBG_OK;
 }
 

@@ -166,6 +166,7 @@ struct StepArgs {
   const uint16_t* blk_runs;
   int64_t n_blocks;
   int32_t* stage_err;
+  int32_t* pipe_ctr;  // next block of the pipelined launch (zeroed before each launch)
   const uint32_t* site_code;
   const uint8_t* block_bulk;  // 1: all 512 slots are bulk sites
   const uint32_t* b_wall;

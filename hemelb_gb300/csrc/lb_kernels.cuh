@@ -6,6 +6,7 @@
 #include "lb_launch.h"
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 // Launch shape of the stream-and-collide kernel (threads per CTA must divide 512;
@@ -833,6 +834,259 @@ void launch_block_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st
     k_stream_collide_block<P, THREADS, MINB><<<(unsigned)a.n_blocks, THREADS, smem, st>>>(a, bxyz);
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined launch (FP32 / FP16 storage): one persistent CTA per SM, a producer
+// warp and NCW consumer warps around a ring of STAGES shared-memory buffers, each
+// holding one 8^3 block's fluid rows of the old distributions.  The producer takes
+// the next block of the z-column order from a global counter (the blocks in
+// flight stay a narrow window of that order, as in a one-shot launch), and stages
+// its rows by bulk asynchronous copies up to STAGES - 1 blocks ahead of the
+// consumers, so the copies in flight do not hold registers and no warp waits on a
+// list entry before its loads.  The consumers collide the block's fluid sites
+// from shared memory, push them and zero-fill the solid slots of the block's
+// fluid rows, as the block-staged launch does, then release the buffer.  Every
+// wait is bounded; a CTA that gives up raises stage_err and lets its copies land
+// before it exits.
+// ---------------------------------------------------------------------------
+// Blocks per fetch of the pipelined launch's counter; HLBG_PIPE_SPAN=1 (default)
+// stages each block as one copy per direction of its rows from the first fluid
+// row to the last (gaps included), 0 as one copy per run of fluid rows (exact
+// bytes, but 2.3 runs per block on the vascular forest: the bulk-copy issue rate
+// then limits the launch).
+#ifndef HLBG_PIPE_CHUNK
+#define HLBG_PIPE_CHUNK 8
+#endif
+#ifndef HLBG_PIPE_SPAN
+#define HLBG_PIPE_SPAN 1
+#endif
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+template <int P, int NCW, int STAGES>
+__global__ void __launch_bounds__((NCW + 1) * 32, 1) k_stream_collide_pipe(StepArgs a, const int32_t* block_xyz) {
+  static_assert(P != 0, "the staged block holds FP32 or FP16 values");
+  using S = typename Store<P>::S;
+  using T = typename Calc<P>::T;
+  constexpr int kStage = Q * kSites;  // values per buffer
+  extern __shared__ __align__(128) unsigned char pipe_raw[];
+  S* ring = reinterpret_cast<S*>(pipe_raw);
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
+  __shared__ int32_t st_block[STAGES];
+  __shared__ uint32_t st_wfl[STAGES][16], st_wbd[STAGES][16], st_pre[STAGES][17];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < STAGES; ++k) {
+      mbar_init(smem_u32(&full_bar[k]), 1);
+      mbar_init(smem_u32(&empty_bar[k]), NCW);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (warp == 0) {
+    // ---- producer ----
+    // Blocks come in chunks of CH consecutive blocks per counter fetch; the chunk's
+    // run offsets, bitmaps and runs are loaded into shared memory (two dependent
+    // rounds of loads for CH blocks) before the producer waits for free buffers.
+    constexpr int CH = HLBG_PIPE_CHUNK;
+    __shared__ uint32_t p_roff[CH + 1], p_wfl[CH * 16], p_wbd[CH * 16];
+    __shared__ uint16_t p_runs[CH * 32];
+    int k = 0;
+    bool ok = true;
+    for (bool more = true; more && ok;) {
+      int32_t c0 = 0;
+      if (lane == 0) c0 = atomicAdd(a.pipe_ctr, CH);
+      c0 = __shfl_sync(0xffffffffu, c0, 0);
+      const int nch = c0 < a.n_blocks ? (a.n_blocks - c0 < CH ? (int)(a.n_blocks - c0) : CH) : 0;
+      if (lane <= nch && nch > 0) p_roff[lane] = __ldg(a.blk_run_off + c0 + lane);
+      for (int i = lane; i < nch * 16; i += 32) {
+        p_wfl[i] = __ldg(reinterpret_cast<const uint32_t*>(a.blk_fluid + (int64_t)c0 * 8) + i);
+        p_wbd[i] = __ldg(reinterpret_cast<const uint32_t*>(a.blk_bnd + (int64_t)c0 * 8) + i);
+      }
+      __syncwarp();
+      const uint32_t R0 = nch > 0 ? p_roff[0] : 0u, R = nch > 0 ? p_roff[nch] - R0 : 0u;
+      for (uint32_t i = lane; i < R; i += 32) p_runs[i] = __ldg(a.blk_runs + R0 + i);
+      __syncwarp();
+      for (int i = 0; i <= nch && i < CH + 1; ++i, ++k) {
+        if (i == nch && nch == CH) break;  // a full chunk: fetch the next one
+        const int sb = k % STAGES;
+        if (k >= STAGES && !mbar_wait(smem_u32(&empty_bar[sb]), ((k / STAGES) - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        if (i == nch) {  // the blocks are used up: the consumers stop here
+          if (lane == 0) {
+            st_block[sb] = -1;
+            mbar_arrive(smem_u32(&full_bar[sb]));
+          }
+          ++k;
+          more = false;
+          break;
+        }
+        const int64_t b = c0 + i;
+        // the block's fluid / boundary bitmaps and the prefix counts of its fluid words
+        const uint32_t wf = lane < 16 ? p_wfl[i * 16 + lane] : 0u;
+        uint32_t incl = __popc(wf);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        if (lane < 16) {
+          st_wfl[sb][lane] = wf;
+          st_wbd[sb][lane] = p_wbd[i * 16 + lane];
+          st_pre[sb][lane] = incl - __popc(wf);
+        }
+        if (lane == 16) st_pre[sb][16] = incl;  // lanes 16.. add nothing: the total
+        // the copies: (run, direction) pairs over the lanes; sizes and both addresses
+        // are multiples of 16 bytes (rows of 8 values of 2 or 4 bytes)
+        const uint32_t r0 = p_roff[i] - R0, r1 = p_roff[i + 1] - R0;
+#if HLBG_PIPE_SPAN
+        // one copy per direction of the rows from the first fluid row to the last
+        const uint32_t row0 = r1 > r0 ? (p_runs[r0] & 63u) : 0u;
+        const uint32_t rowe = r1 > r0 ? (p_runs[r1 - 1] & 63u) + (p_runs[r1 - 1] >> 6) : 0u;
+        const uint32_t bytes = (rowe - row0) * 8u * (uint32_t)(Q * sizeof(S));
+#else
+        uint32_t bytes = 0;
+        for (uint32_t r = r0 + lane; r < r1; r += 32) bytes += (uint32_t)(p_runs[r] >> 6) * 8u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+        bytes *= (uint32_t)(Q * sizeof(S));
+#endif
+        if (lane == 0) st_block[sb] = (int32_t)b;
+        __syncwarp();
+        if (lane == 0)
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(&full_bar[sb])),
+                       "r"(bytes)
+                       : "memory");
+        __syncwarp();
+        const char* src0 = static_cast<const char*>(a.f_old) + (size_t)b * kStage * sizeof(S);
+        const uint32_t dst0 = smem_u32(ring + (size_t)sb * kStage);
+#if HLBG_PIPE_SPAN
+        const uint32_t ncopy = rowe > row0 ? Q : 0u;
+#else
+        const uint32_t ncopy = (r1 - r0) * Q;
+#endif
+        for (uint32_t c = lane; c < ncopy; c += 32) {
+#if HLBG_PIPE_SPAN
+          const uint32_t run = row0 | ((rowe - row0) << 6), d = c;
+#else
+          const uint32_t run = p_runs[r0 + c / Q], d = c % Q;
+#endif
+          const uint32_t off = (d * kSites + (run & 63u) * 8u) * (uint32_t)sizeof(S);
+          const uint32_t size = (run >> 6) * 8u * (uint32_t)sizeof(S);
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                  dst0 + off),
+              "l"(src0 + off), "r"(size), "r"(smem_u32(&full_bar[sb]))
+              : "memory");
+        }
+      }
+      __syncwarp();  // the chunk's scratch is reused by the next fetch
+    }
+    if (!ok) {
+      if (lane == 0) atomicExch(a.stage_err, 1);
+      // every copy armed so far has to land before the CTA may exit
+      for (int j = k - STAGES > 0 ? k - STAGES : 0; j < k; ++j) mbar_wait(smem_u32(&full_bar[j % STAGES]), (j / STAGES) & 1);
+    }
+    return;
+  }
+  // ---- consumers ----
+  const int cw = warp - 1;
+  MonAccT<P> acc = mon_neutral_t<P>();  // unused: pipelined steps are not monitored
+  const MonOld<P> uo;
+  S* fn = static_cast<S*>(a.f_new);
+  int rot = 0;  // tasks of the earlier blocks, mod NCW
+  for (int k = 0;; ++k) {
+    const int sb = k % STAGES;
+    if (!mbar_wait(smem_u32(&full_bar[sb]), (k / STAGES) & 1)) {
+      if (lane == 0) atomicExch(a.stage_err, 1);
+      return;
+    }
+    const int64_t b = st_block[sb];
+    if (b < 0) return;
+    const S* stage = ring + (size_t)sb * kStage;
+    const uint32_t* wfl = st_wfl[sb];
+    const uint32_t* wbd = st_wbd[sb];
+    const uint32_t* pre = st_pre[sb];
+    const int nf = (int)pre[16];
+    // the block's tasks: 32-site collide units, then (partly fluid blocks) 32-slot
+    // zero-fill units; task t of the launch's running count goes to consumer warp
+    // t mod NCW, so every warp takes the same share whatever the blocks' sizes
+    const int ncol = (nf + 31) >> 5;
+    const int ntask = ncol + (nf < kSites ? kSites / 32 : 0);
+    const int first = ((cw - rot) % NCW + NCW) % NCW;
+    const int32_t tabreg = lane < 27 && first < ncol ? __ldg(a.block_nbr + b * 27 + lane) : 0;
+    for (int task = first; task < ntask; task += NCW) {  // warp-uniform trips
+      if (task >= ncol) {
+        // solid slots of the rows that hold fluid: zeros complete their sectors
+        const int j = (task - ncol) * 32 + lane;
+        const uint32_t w = wfl[j >> 5];
+        if (((w >> (j & 24)) & 0xffu) != 0 && !((w >> (j & 31)) & 1u)) {
+#pragma unroll
+          for (int d = 0; d < Q; ++d) Store<P>::store(fn, fidx(b * kSites + j, d), (T)0, a);
+        }
+        continue;
+      }
+      const int t = task * 32 + lane;
+      const bool on = t < nf;
+      int j = 0;
+      if (on) {
+        int w = 0;  // the word holding the t-th fluid slot
+#pragma unroll
+        for (int h = 8; h > 0; h >>= 1)
+          if ((int)pre[w + h] <= t) w += h;
+        j = w * 32 + select32(wfl[w], t - (int)pre[w]);
+      }
+      const int64_t s = b * kSites + j;
+      const bool bnd = on && ((wbd[j >> 5] >> (j & 31)) & 1u);
+      const uint32_t code = on ? (bnd ? a.site_code[s] : 1u) : 0u;
+      T f[Q];
+#pragma unroll
+      for (int d = 0; d < Q; ++d) {
+        if constexpr (P == 1)
+          f[d] = on ? stage[d * kSites + j] : 0.f;
+        else
+          f[d] = on ? __half2float(stage[d * kSites + j]) * a.fp16_inv_scale : 0.f;
+      }
+      collide_and_push<P, false>(a, b, j, s, j, code, tabreg, f, block_xyz, acc, false, uo);
+    }
+    rot = (rot + ntask) % NCW;
+    __syncwarp();
+    if (lane == 0) mbar_arrive(smem_u32(&empty_bar[sb]));
+  }
+}
+
+#ifndef HLBG_PIPE_NCW
+#define HLBG_PIPE_NCW 31
+#endif
+#ifndef HLBG_PIPE_STAGES
+#define HLBG_PIPE_STAGES 4
+#endif
+
+template <int P, int NCW, int STAGES>
+void launch_pipe(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
+  constexpr size_t smem = (size_t)STAGES * Q * kSites * sizeof(typename Store<P>::S);
+  static std::atomic<bool> configured[64];
+  static int sms[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!configured[dev].load()) {  // per device: the attribute belongs to the current context
+    cudaFuncSetAttribute(k_stream_collide_pipe<P, NCW, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    configured[dev].store(true);
+  }
+  if (a.n_blocks <= 0) return;
+  cudaMemsetAsync(a.pipe_ctr, 0, sizeof(int32_t), st);
+  const int64_t grid = std::min<int64_t>(sms[dev] > 0 ? sms[dev] : 1, a.n_blocks);
+  k_stream_collide_pipe<P, NCW, STAGES><<<(unsigned)grid, (NCW + 1) * 32, smem, st>>>(a, bxyz);
+}
+
 // Resident CTAs per SM of the 128-thread fluid-list launch (variant 6) in plain steps.
 #ifndef HLBG_LIST_MINB
 #define HLBG_LIST_MINB 8
@@ -1433,6 +1687,15 @@ __global__ void k_halo_unpack(void* f, const int64_t* off, int64_t n, int64_t li
       }                                                                                         \
       variant = 6; /* FP64, or a layout without the block tables */                             \
     }                                                                                           \
+    if (variant == 8) {                                                                         \
+      if constexpr (P != 0) {                                                                   \
+        if (a.blk_runs && !a.mon_u) {                                                           \
+          launch_pipe<P, HLBG_PIPE_NCW, (P == 1 ? HLBG_PIPE_STAGES : 2 * HLBG_PIPE_STAGES)>(a, bxyz, st); \
+          return;                                                                               \
+        }                                                                                       \
+      }                                                                                         \
+      variant = 6; /* FP64, monitored steps, or a layout without the block tables */            \
+    }                                                                                           \
     if (variant == 5) {                                                                         \
       launch_listed<P, 128, (P == 0 ? 2 : 9), false>(a, bxyz, st);                              \
       return;                                                                                   \
@@ -1469,7 +1732,7 @@ __global__ void k_halo_unpack(void* f, const int64_t* off, int64_t n, int64_t li
     }                                                                                           \
   }                                                                                             \
   int64_t monitored_grid_##P(int64_t nslot, int variant, int64_t n_warps) {                    \
-    if (variant >= 4) return (n_warps * 32 + 127) / 128; /* monitored 4..7 run as 6 */          \
+    if (variant >= 4) return (n_warps * 32 + 127) / 128; /* monitored 4..8 run as 6 */          \
     if (P == 0) return nslot / 128;                                                             \
     switch (variant) {                                                                          \
       case 1: return nslot / 128;                                                               \

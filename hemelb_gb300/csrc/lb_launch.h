@@ -11,8 +11,9 @@ struct StepArgs;
 
 // Launch variants of the stream-and-collide kernel (FP32 / FP16 forms; FP64 has one):
 // 0 default shape, 1: 128x8, 2: 256x4, 3: 512x2 threads x resident CTAs per SM,
-// 4: persistent 128-thread CTAs striding over the slots.
-constexpr int kSCVariants = 8;  // 5, 6: the fluid-list launch; 7: staged (FP32)
+// 4: one CTA per block, staged by bulk copies; 5, 6, 7: the fluid-list launch;
+// 8: persistent, pipelined block staging (FP32 / FP16).
+constexpr int kSCVariants = 9;
 
 struct PostArgs {
   void* f_new;

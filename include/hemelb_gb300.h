@@ -310,12 +310,15 @@ int hlbg_incompressibility(hlbg_ctx *ctx, hlbg_incomp *out);
  * (-1)^(z+t) j_z, and likewise for x and y), which otherwise decays only through
  * the iolets and dominates the time to steady state. */
 int hlbg_average_time_levels(hlbg_ctx *ctx);
-/* Select the stream-and-collide launch shape by index (0..7: all slots at 128x10,
+/* Select the stream-and-collide launch shape by index (0..8: all slots at 128x10,
  * 128x8, 256x4, 512x2 threads x resident CTAs; one CTA per block with the block's
  * fluid rows staged in shared memory by bulk asynchronous copies (FP32 / FP16;
  * FP64 runs index 6 instead); the fluid list, whose warps hold only fluid slots,
- * at 128x9, 128x8 and 64x16); FP64 runs two CTAs per SM.  Monitored steps run
- * every index from 4 up as the 128x8 fluid list.  No reference counterpart. */
+ * at 128x9, 128x8 and 64x16; one persistent CTA per SM whose producer warp stages
+ * blocks into a ring of shared-memory buffers by bulk asynchronous copies ahead of
+ * 31 consumer warps (FP32 / FP16; FP64 runs index 6 instead)); FP64 runs two
+ * CTAs per SM.  Monitored steps run every index from 4 up as the 128x8 fluid
+ * list.  No reference counterpart. */
 int hlbg_set_launch_variant(hlbg_ctx *ctx, int32_t variant);
 /* Autotuner: time each launch shape / schedule of the stream-and-collide kernel
  * (threads per CTA x resident CTAs per SM, per-slot grid or persistent grid) on

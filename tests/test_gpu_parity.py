@@ -282,7 +282,7 @@ def test_every_launch_shape_gives_identical_distributions(precision):
     candidates) computes the same update: identical arrays after 200 steps."""
     c = small_bifurcation()
     ref = None
-    for v in range(8):
+    for v in range(9):
         s = c.solver(precision)
         s.SetLaunchVariant(v)
         s.SetInitialConditions()
