@@ -94,6 +94,13 @@ def ensemble_report(n_members: int = 512, steps: int = 50, warmup: int = 5, seed
     t_setup = time.perf_counter() - t0
     s.SetInitialConditions()
     variant, tuned_ms = s.autotune(5)
+    # every candidate's step time on this workload (the same update bit for bit)
+    per_variant = {}
+    for v in range(9):
+        s.SetLaunchVariant(v)
+        s.DoTimeStep(1)
+        per_variant[v] = s.time_steps(10) / 10
+    s.SetLaunchVariant(variant)
     s.DoTimeStepGraph(warmup)
     ms = C.c_float()
     capi.check(lib.hlbg_sync(s.ctx), s.ctx)
@@ -128,6 +135,7 @@ def ensemble_report(n_members: int = 512, steps: int = 50, warmup: int = 5, seed
             "fluid_sites": int(n), "steps": steps,
             "batched": {"mlups": n * steps / batched_s / 1e6, "seconds": batched_s,
                         "autotuned_variant": variant, "tuned_ms_per_step": tuned_ms,
+                        "ms_per_step_by_variant": per_variant,
                         "setup_s": t_setup, "stable": bool(st.unstable_sites == 0)},
             "sequential": {"mlups": seq_sites * steps / seq_s / 1e6, "seconds": seq_s},
             "speedup": (n * steps / batched_s) / (seq_sites * steps / seq_s)}
