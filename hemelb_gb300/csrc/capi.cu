@@ -144,6 +144,7 @@ struct hlbg_ctx {
   uint64_t* d_blk_bnd = nullptr;
   uint32_t* d_blk_run_off = nullptr;
   uint16_t* d_blk_runs = nullptr;
+  uint64_t* d_pipe_desc = nullptr;  // pipelined launch: per block, its fluid-list warps and row span
   int32_t* d_stage_err = nullptr;
   std::vector<int32_t> h_flux_slot, h_flux_gi;  // sites with iolet links, their iolet
   int32_t* d_flux_slot = nullptr;
@@ -270,6 +271,7 @@ void fill_args(hlbg_ctx* ctx, StepArgs& a) {
   a.blk_bnd = ctx->d_blk_bnd;
   a.blk_run_off = ctx->d_blk_run_off;
   a.blk_runs = ctx->d_blk_runs;
+  a.pipe_desc = ctx->d_pipe_desc;
   a.n_blocks = ctx->nb;
   a.stage_err = ctx->d_stage_err;
   a.pipe_ctr = ctx->d_stage_err + 1;
@@ -707,7 +709,20 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
       tmp.clear();
     };
     const int split = HLBG_LIST_SPLIT < 0 ? (ctx->prec == HLBG_FP16 ? 1 : 0) : HLBG_LIST_SPLIT;
+    // pipelined launch, per block: its first list warp (bits 0-31), the span of
+    // rows from its first fluid row to its last (32-37: first, 38-44: end), its
+    // fluid warps (45-50) and zero-fill warps (51-56)
+    std::vector<uint64_t> desc((size_t)nb, 0);
     for (int64_t b = 0; b < nb; ++b) {
+      const uint64_t first = wb.size();
+      int row0 = 64, rowe = 0;
+      for (int row = 0; row < 64; ++row)
+        for (int t = 0; t < 8; ++t)
+          if (code[b * 512 + row * 8 + t]) {
+            row0 = std::min(row0, row);
+            rowe = row + 1;
+          }
+      if (rowe == 0) row0 = 0;
       if (split == 1) {
         // bulk sites first, then the boundary sites, so that most warps take the
         // bulk push path and only the warps holding boundary sites the mixed one
@@ -733,6 +748,7 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
           if (code[b * 512 + j]) tmp.push_back((uint16_t)(j | (code[b * 512 + j] >= 2 ? kListBoundary : 0u)));
       }
       flush(b, false);
+      const uint64_t nfw = wb.size() - first;
       for (int sec = 0; sec < 64; ++sec) {
         bool any = false;
         for (int t = 0; t < 8; ++t) any |= code[b * 512 + sec * 8 + t] != 0;
@@ -741,10 +757,15 @@ int build_layout(hlbg_ctx* ctx, const hlbg_geometry* g) {
           if (!code[b * 512 + sec * 8 + t]) tmp.push_back((uint16_t)(sec * 8 + t));
       }
       flush(b, true);
+      const uint64_t nzw = wb.size() - first - nfw;
+      desc[b] = first | ((uint64_t)row0 << 32) | ((uint64_t)rowe << 38) | (nfw << 45) | (nzw << 51);
     }
     ctx->n_warps = (int64_t)wb.size();
     if ((rc = upload(ctx, &ctx->d_warp_block, wb))) return rc;
     if ((rc = upload(ctx, &ctx->d_lane_slot, ls))) return rc;
+    if (!HLBG_PACK && !HLBG_BLOCK_ORDER && ctx->n_warps < (int64_t)1 << 32 &&
+        (rc = upload(ctx, &ctx->d_pipe_desc, desc)))
+      return rc;
   }
   if (!HLBG_PACK && !HLBG_BLOCK_ORDER) {
     // block-staged launch: fluid / boundary bitmaps per block (slot order) and the
@@ -1064,7 +1085,7 @@ void hlbg_destroy(hlbg_ctx* ctx) {
                   ctx->d_steady_n,  ctx->d_slot2site, ctx->d_site2slot, ctx->d_mon_u,
                   ctx->d_mon_part,  ctx->d_mon_part2, ctx->d_mon_state, ctx->d_mon_result,
                   ctx->d_warp_block, ctx->d_lane_slot, ctx->d_b_normal, ctx->d_wss,
-                  ctx->d_blk_fluid, ctx->d_blk_bnd, ctx->d_blk_run_off, ctx->d_blk_runs, ctx->d_stage_err,
+                  ctx->d_blk_fluid, ctx->d_blk_bnd, ctx->d_blk_run_off, ctx->d_blk_runs, ctx->d_pipe_desc, ctx->d_stage_err,
                   ctx->d_flux_slot, ctx->d_flux_gi, ctx->d_flux, ctx->d_halo_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);

@@ -164,6 +164,7 @@ struct StepArgs {
   const uint64_t* blk_bnd;
   const uint32_t* blk_run_off;
   const uint16_t* blk_runs;
+  const uint64_t* pipe_desc;  // pipelined launch: per block, its list warps and row span
   int64_t n_blocks;
   int32_t* stage_err;
   int32_t* pipe_ctr;  // next block of the pipelined launch (zeroed before each launch)

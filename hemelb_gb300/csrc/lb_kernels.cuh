@@ -837,27 +837,23 @@ void launch_block_staged(const StepArgs& a, const int32_t* bxyz, cudaStream_t st
 // ---------------------------------------------------------------------------
 // Pipelined launch (FP32 / FP16 storage): one persistent CTA per SM, a producer
 // warp and NCW consumer warps around a ring of STAGES shared-memory buffers, each
-// holding one 8^3 block's fluid rows of the old distributions.  The producer takes
-// the next block of the z-column order from a global counter (the blocks in
-// flight stay a narrow window of that order, as in a one-shot launch), and stages
-// its rows by bulk asynchronous copies up to STAGES - 1 blocks ahead of the
-// consumers, so the copies in flight do not hold registers and no warp waits on a
-// list entry before its loads.  The consumers collide the block's fluid sites
-// from shared memory, push them and zero-fill the solid slots of the block's
-// fluid rows, as the block-staged launch does, then release the buffer.  Every
-// wait is bounded; a CTA that gives up raises stage_err and lets its copies land
-// before it exits.
+// holding one 8^3 block: its rows of the old distributions from the first fluid
+// row to the last (one bulk copy per direction) and its warps of the fluid list
+// (the same lane entries the fluid-list launch reads).  The producer takes chunks
+// of consecutive blocks of the z-column order from a global counter (the blocks
+// in flight stay a narrow window of that order, as in a one-shot launch), reads
+// their descriptors (pipe_desc: first list warp, row span, fluid and zero-fill
+// warps) and stages each block up to STAGES - 1 blocks ahead of the consumers,
+// so the copies in flight hold no registers and no warp waits on a list entry or
+// a distribution in DRAM.  The consumers take the staged block's list warps
+// round-robin (warp task t of the launch to consumer warp t mod NCW), collide and
+// push exactly as a fluid-list warp does, zero-fill as its zero-fill warps do,
+// and release the buffer.  Every wait is bounded; a CTA that gives up raises
+// stage_err and lets its copies land before it exits.
 // ---------------------------------------------------------------------------
-// Blocks per fetch of the pipelined launch's counter; HLBG_PIPE_SPAN=1 (default)
-// stages each block as one copy per direction of its rows from the first fluid
-// row to the last (gaps included), 0 as one copy per run of fluid rows (exact
-// bytes, but 2.3 runs per block on the vascular forest: the bulk-copy issue rate
-// then limits the launch).
+// Blocks per fetch of the pipelined launch's counter.
 #ifndef HLBG_PIPE_CHUNK
 #define HLBG_PIPE_CHUNK 8
-#endif
-#ifndef HLBG_PIPE_SPAN
-#define HLBG_PIPE_SPAN 1
 #endif
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
@@ -865,18 +861,30 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
 }
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// Bytes of one ring buffer: the distributions of a whole block, then up to 32
+// list warps (16 fluid + 16 zero-fill) of 32 uint16 entries.
+template <int P>
+struct PipeStage {
+  static constexpr uint32_t kValues = (uint32_t)(Q * kSites * sizeof(typename Store<P>::S));
+  static constexpr uint32_t kBytes = kValues + 32 * 32 * 2;
+};
 
 template <int P, int NCW, int STAGES>
 __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_stream_collide_pipe(StepArgs a, const int32_t* block_xyz) {
   static_assert(P != 0, "the staged block holds FP32 or FP16 values");
   using S = typename Store<P>::S;
   using T = typename Calc<P>::T;
-  constexpr int kStage = Q * kSites;  // values per buffer
+  using PS = PipeStage<P>;
   extern __shared__ __align__(128) unsigned char pipe_raw[];
-  S* ring = reinterpret_cast<S*>(pipe_raw);
   __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES];
   __shared__ int32_t st_block[STAGES];
-  __shared__ uint32_t st_wfl[STAGES][16], st_wbd[STAGES][16], st_pre[STAGES][17];
+  __shared__ uint32_t st_warps[STAGES];  // fluid warps | zero-fill warps << 8
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int k = 0; k < STAGES; ++k) {
@@ -888,12 +896,7 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_stream_collide_pipe(StepA
   __syncthreads();
   if (warp == 0) {
     // ---- producer ----
-    // Blocks come in chunks of CH consecutive blocks per counter fetch; the chunk's
-    // run offsets, bitmaps and runs are loaded into shared memory (two dependent
-    // rounds of loads for CH blocks) before the producer waits for free buffers.
     constexpr int CH = HLBG_PIPE_CHUNK;
-    __shared__ uint32_t p_roff[CH + 1], p_wfl[CH * 16], p_wbd[CH * 16];
-    __shared__ uint16_t p_runs[CH * 32];
     int k = 0;
     bool ok = true;
     for (bool more = true; more && ok;) {
@@ -901,91 +904,55 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_stream_collide_pipe(StepA
       if (lane == 0) c0 = atomicAdd(a.pipe_ctr, CH);
       c0 = __shfl_sync(0xffffffffu, c0, 0);
       const int nch = c0 < a.n_blocks ? (a.n_blocks - c0 < CH ? (int)(a.n_blocks - c0) : CH) : 0;
-      if (lane <= nch && nch > 0) p_roff[lane] = __ldg(a.blk_run_off + c0 + lane);
-      for (int i = lane; i < nch * 16; i += 32) {
-        p_wfl[i] = __ldg(reinterpret_cast<const uint32_t*>(a.blk_fluid + (int64_t)c0 * 8) + i);
-        p_wbd[i] = __ldg(reinterpret_cast<const uint32_t*>(a.blk_bnd + (int64_t)c0 * 8) + i);
-      }
-      __syncwarp();
-      const uint32_t R0 = nch > 0 ? p_roff[0] : 0u, R = nch > 0 ? p_roff[nch] - R0 : 0u;
-      for (uint32_t i = lane; i < R; i += 32) p_runs[i] = __ldg(a.blk_runs + R0 + i);
-      __syncwarp();
-      for (int i = 0; i <= nch && i < CH + 1; ++i, ++k) {
-        if (i == nch && nch == CH) break;  // a full chunk: fetch the next one
+      // the chunk's descriptors, one per lane
+      const uint64_t mine = lane < nch ? __ldg(a.pipe_desc + c0 + lane) : 0ull;
+      for (int i = 0; i < nch; ++i, ++k) {
         const int sb = k % STAGES;
         if (k >= STAGES && !mbar_wait(smem_u32(&empty_bar[sb]), ((k / STAGES) - 1) & 1)) {
           ok = false;
           break;
         }
-        if (i == nch) {  // the blocks are used up: the consumers stop here
+        const uint64_t dsc = __shfl_sync(0xffffffffu, mine, i);
+        const int64_t b = c0 + i;
+        const uint32_t first = (uint32_t)dsc;
+        const uint32_t row0 = (uint32_t)(dsc >> 32) & 63u, rowe = (uint32_t)(dsc >> 38) & 127u;
+        const uint32_t nfw = (uint32_t)(dsc >> 45) & 63u, nzw = (uint32_t)(dsc >> 51) & 63u;
+        const uint32_t span = (rowe - row0) * 8u * (uint32_t)sizeof(S);
+        const uint32_t lbytes = (nfw + nzw) * 64u;
+        if (lane == 0) {
+          st_block[sb] = (int32_t)b;
+          st_warps[sb] = nfw | (nzw << 8);
+        }
+        __syncwarp();
+        const uint32_t bar = smem_u32(&full_bar[sb]);
+        if (lane == 0)
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                       "r"(span * Q + lbytes)
+                       : "memory");
+        __syncwarp();
+        // sizes and both addresses are multiples of 16 bytes (rows of 8 values of 2
+        // or 4 bytes; list warps of 64 bytes)
+        const uint32_t dst0 = smem_u32(pipe_raw) + (uint32_t)sb * PS::kBytes;
+        if (lane < Q && span > 0) {
+          const uint32_t off = ((uint32_t)lane * kSites + row0 * 8u) * (uint32_t)sizeof(S);
+          bulk_copy(dst0 + off, static_cast<const char*>(a.f_old) + (size_t)b * Q * kSites * sizeof(S) + off, span,
+                    bar);
+        }
+        if (lane == Q && lbytes > 0) bulk_copy(dst0 + PS::kValues, a.lane_slot + (size_t)first * 32, lbytes, bar);
+      }
+      if (ok && nch < CH) {  // the blocks are used up: the consumers stop at the next buffer
+        const int sb = k % STAGES;
+        if (k >= STAGES && !mbar_wait(smem_u32(&empty_bar[sb]), ((k / STAGES) - 1) & 1)) {
+          ok = false;
+        } else {
           if (lane == 0) {
             st_block[sb] = -1;
             mbar_arrive(smem_u32(&full_bar[sb]));
           }
           ++k;
-          more = false;
-          break;
         }
-        const int64_t b = c0 + i;
-        // the block's fluid / boundary bitmaps and the prefix counts of its fluid words
-        const uint32_t wf = lane < 16 ? p_wfl[i * 16 + lane] : 0u;
-        uint32_t incl = __popc(wf);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += v;
-        }
-        if (lane < 16) {
-          st_wfl[sb][lane] = wf;
-          st_wbd[sb][lane] = p_wbd[i * 16 + lane];
-          st_pre[sb][lane] = incl - __popc(wf);
-        }
-        if (lane == 16) st_pre[sb][16] = incl;  // lanes 16.. add nothing: the total
-        // the copies: (run, direction) pairs over the lanes; sizes and both addresses
-        // are multiples of 16 bytes (rows of 8 values of 2 or 4 bytes)
-        const uint32_t r0 = p_roff[i] - R0, r1 = p_roff[i + 1] - R0;
-#if HLBG_PIPE_SPAN
-        // one copy per direction of the rows from the first fluid row to the last
-        const uint32_t row0 = r1 > r0 ? (p_runs[r0] & 63u) : 0u;
-        const uint32_t rowe = r1 > r0 ? (p_runs[r1 - 1] & 63u) + (p_runs[r1 - 1] >> 6) : 0u;
-        const uint32_t bytes = (rowe - row0) * 8u * (uint32_t)(Q * sizeof(S));
-#else
-        uint32_t bytes = 0;
-        for (uint32_t r = r0 + lane; r < r1; r += 32) bytes += (uint32_t)(p_runs[r] >> 6) * 8u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
-        bytes *= (uint32_t)(Q * sizeof(S));
-#endif
-        if (lane == 0) st_block[sb] = (int32_t)b;
-        __syncwarp();
-        if (lane == 0)
-          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(&full_bar[sb])),
-                       "r"(bytes)
-                       : "memory");
-        __syncwarp();
-        const char* src0 = static_cast<const char*>(a.f_old) + (size_t)b * kStage * sizeof(S);
-        const uint32_t dst0 = smem_u32(ring + (size_t)sb * kStage);
-#if HLBG_PIPE_SPAN
-        const uint32_t ncopy = rowe > row0 ? Q : 0u;
-#else
-        const uint32_t ncopy = (r1 - r0) * Q;
-#endif
-        for (uint32_t c = lane; c < ncopy; c += 32) {
-#if HLBG_PIPE_SPAN
-          const uint32_t run = row0 | ((rowe - row0) << 6), d = c;
-#else
-          const uint32_t run = p_runs[r0 + c / Q], d = c % Q;
-#endif
-          const uint32_t off = (d * kSites + (run & 63u) * 8u) * (uint32_t)sizeof(S);
-          const uint32_t size = (run >> 6) * 8u * (uint32_t)sizeof(S);
-          asm volatile(
-              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-                  dst0 + off),
-              "l"(src0 + off), "r"(size), "r"(smem_u32(&full_bar[sb]))
-              : "memory");
-        }
+        more = false;
       }
-      __syncwarp();  // the chunk's scratch is reused by the next fetch
     }
     if (!ok) {
       if (lane == 0) atomicExch(a.stage_err, 1);
@@ -999,7 +966,7 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_stream_collide_pipe(StepA
   MonAccT<P> acc = mon_neutral_t<P>();  // unused: pipelined steps are not monitored
   const MonOld<P> uo;
   S* fn = static_cast<S*>(a.f_new);
-  int rot = 0;  // tasks of the earlier blocks, mod NCW
+  int rot = 0;  // list warps of the earlier blocks, mod NCW
   for (int k = 0;; ++k) {
     const int sb = k % STAGES;
     if (!mbar_wait(smem_u32(&full_bar[sb]), (k / STAGES) & 1)) {
@@ -1008,42 +975,24 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_stream_collide_pipe(StepA
     }
     const int64_t b = st_block[sb];
     if (b < 0) return;
-    const S* stage = ring + (size_t)sb * kStage;
-    const uint32_t* wfl = st_wfl[sb];
-    const uint32_t* wbd = st_wbd[sb];
-    const uint32_t* pre = st_pre[sb];
-    const int nf = (int)pre[16];
-    // the block's tasks: 32-site collide units, then (partly fluid blocks) 32-slot
-    // zero-fill units; task t of the launch's running count goes to consumer warp
-    // t mod NCW, so every warp takes the same share whatever the blocks' sizes
-    const int ncol = (nf + 31) >> 5;
-    const int ntask = ncol + (nf < kSites ? kSites / 32 : 0);
+    const S* stage = reinterpret_cast<const S*>(pipe_raw + (size_t)sb * PS::kBytes);
+    const uint16_t* list = reinterpret_cast<const uint16_t*>(pipe_raw + (size_t)sb * PS::kBytes + PS::kValues);
+    const int nfw = (int)(st_warps[sb] & 0xffu), ntask = nfw + (int)(st_warps[sb] >> 8);
     const int first = ((cw - rot) % NCW + NCW) % NCW;
-    const int32_t tabreg = lane < 27 && first < ncol ? __ldg(a.block_nbr + b * 27 + lane) : 0;
+    const int32_t tabreg = lane < 27 && first < nfw ? __ldg(a.block_nbr + b * 27 + lane) : 0;
     for (int task = first; task < ntask; task += NCW) {  // warp-uniform trips
-      if (task >= ncol) {
-        // solid slots of the rows that hold fluid: zeros complete their sectors
-        const int j = (task - ncol) * 32 + lane;
-        const uint32_t w = wfl[j >> 5];
-        if (((w >> (j & 24)) & 0xffu) != 0 && !((w >> (j & 31)) & 1u)) {
+      const unsigned js = list[task * 32 + lane];
+      const bool on = js != 0xffffu;
+      const int j = on ? (int)(js & (kSites - 1)) : 0;
+      const int64_t s = b * kSites + j;
+      if (task >= nfw) {  // zero-fill warp: complete the sectors its slots share with fluid
+        if (on) {
 #pragma unroll
-          for (int d = 0; d < Q; ++d) Store<P>::store(fn, fidx(b * kSites + j, d), (T)0, a);
+          for (int d = 0; d < Q; ++d) Store<P>::store(fn, fidx(s, d), (T)0, a);
         }
         continue;
       }
-      const int t = task * 32 + lane;
-      const bool on = t < nf;
-      int j = 0;
-      if (on) {
-        int w = 0;  // the word holding the t-th fluid slot
-#pragma unroll
-        for (int h = 8; h > 0; h >>= 1)
-          if ((int)pre[w + h] <= t) w += h;
-        j = w * 32 + select32(wfl[w], t - (int)pre[w]);
-      }
-      const int64_t s = b * kSites + j;
-      const bool bnd = on && ((wbd[j >> 5] >> (j & 31)) & 1u);
-      const uint32_t code = on ? (bnd ? a.site_code[s] : 1u) : 0u;
+      const uint32_t code = on ? ((js & kListBoundary) ? a.site_code[s] : 1u) : 0u;
       T f[Q];
 #pragma unroll
       for (int d = 0; d < Q; ++d) {
@@ -1069,7 +1018,7 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_stream_collide_pipe(StepA
 
 template <int P, int NCW, int STAGES>
 void launch_pipe(const StepArgs& a, const int32_t* bxyz, cudaStream_t st) {
-  constexpr size_t smem = (size_t)STAGES * Q * kSites * sizeof(typename Store<P>::S);
+  constexpr size_t smem = (size_t)STAGES * PipeStage<P>::kBytes;
   static std::atomic<bool> configured[64];
   static int sms[64];
   int dev = 0;
@@ -1689,7 +1638,7 @@ __global__ void k_halo_unpack(void* f, const int64_t* off, int64_t n, int64_t li
     }                                                                                           \
     if (variant == 8) {                                                                         \
       if constexpr (P != 0) {                                                                   \
-        if (a.blk_runs && !a.mon_u) {                                                           \
+        if (a.pipe_desc && !a.mon_u) {                                                          \
           launch_pipe<P, HLBG_PIPE_NCW, (P == 1 ? HLBG_PIPE_STAGES : 2 * HLBG_PIPE_STAGES)>(a, bxyz, st); \
           return;                                                                               \
         }                                                                                       \
