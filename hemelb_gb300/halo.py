@@ -103,3 +103,91 @@ class Halo:
             self.close()
         except Exception:
             pass
+
+
+# ---- transport ------------------------------------------------------------------
+
+def exchange_buffers(send: dict, recv: dict, group=None) -> None:
+    """One exchange over torch.distributed: post every send and every receive (peer
+    -> 1-D tensor; a send list and the matching receive list on the peer have the
+    same length and order), then wait for all of them, as FieldData::SendAndReceive
+    posts its requests before waiting (Code/geometry/FieldData.cc:27-49).  With a
+    backend that moves host memory only (gloo), device tensors travel through host
+    copies; NCCL moves them directly."""
+    import torch
+    import torch.distributed as dist
+    staged = dist.get_backend(group) != "nccl"
+    reqs, keep, landing = [], [], []
+    for peer in sorted(send):
+        t = send[peer]
+        src = t.cpu() if staged and t.is_cuda else t
+        keep.append(src)
+        reqs.append(dist.isend(src, peer, group=group))
+    for peer in sorted(recv):
+        t = recv[peer]
+        dst = torch.empty(t.shape, dtype=t.dtype) if staged and t.is_cuda else t
+        if dst is not t:
+            landing.append((t, dst))
+        reqs.append(dist.irecv(dst, peer, group=group))
+    for r in reqs:
+        r.wait()
+    for t, dst in landing:
+        t.copy_(dst)
+    if any(t.is_cuda for t in recv.values()):
+        torch.cuda.synchronize()  # the receives are complete before the context's stream reads them
+
+
+class HaloExchange:
+    """One rank's update of a partitioned geometry on its own device: the context
+    (an `LBM` on the halo's local geometry) steps every local site; after
+    StreamAndCollide the values its sites streamed into ghost sites are packed on
+    the device in their storage type (hlbg_halo_pack_device), exchanged with the
+    peers (`exchange_buffers`), unpacked into the owned sites they target
+    (hlbg_halo_unpack_device), and then PostStep and the swap run -- the order of
+    lb::LBM around FieldData's exchange (Code/lb/lb.hpp:176-309).  The owned sites
+    then evolve exactly as in one context over the whole geometry."""
+
+    def __init__(self, solver, halo: Halo, group=None):
+        import torch
+        self._lib = lib = capi.load()
+        self.s, self.h, self.group = solver, halo, group
+        self.elem = lib.hlbg_storage_bytes(solver.ctx)
+        self.plans = []
+        for ex in halo.exchanges:
+            so, ro = self._offsets(ex.send), self._offsets(ex.recv)
+            sbuf = torch.empty(len(ex.send) * self.elem, dtype=torch.uint8, device="cuda")
+            rbuf = torch.empty(len(ex.recv) * self.elem, dtype=torch.uint8, device="cuda")
+            self.plans.append((ex.peer, so, ro, sbuf, rbuf))
+
+    def _offsets(self, triples: np.ndarray):
+        import torch
+        b = np.ascontiguousarray(triples[:, 0], dtype=np.int32)
+        d = np.ascontiguousarray(triples[:, 1], dtype=np.int8)
+        t = np.ascontiguousarray(triples[:, 2], dtype=np.int16)
+        out = np.empty(len(triples), dtype=np.int64)
+        capi.check(self._lib.hlbg_halo_offsets(self.s.ctx, b.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               d.ctypes.data_as(C.POINTER(C.c_int8)),
+                                               t.ctypes.data_as(C.POINTER(C.c_int16)), len(triples),
+                                               out.ctypes.data_as(C.POINTER(C.c_int64))), self.s.ctx)
+        return torch.from_numpy(out).cuda()
+
+    def exchange(self) -> None:
+        lib, ctx = self._lib, self.s.ctx
+        for _, so, _, sbuf, _ in self.plans:
+            capi.check(lib.hlbg_halo_pack_device(ctx, C.c_void_p(so.data_ptr()), so.numel(),
+                                                 C.c_void_p(sbuf.data_ptr())), ctx)
+        capi.check(lib.hlbg_sync(ctx), ctx)
+        capi.check(lib.hlbg_halo_check(ctx), ctx)
+        exchange_buffers({p[0]: p[3] for p in self.plans}, {p[0]: p[4] for p in self.plans}, self.group)
+        for _, _, ro, _, rbuf in self.plans:
+            capi.check(lib.hlbg_halo_unpack_device(ctx, C.c_void_p(ro.data_ptr()), ro.numel(),
+                                                   C.c_void_p(rbuf.data_ptr())), ctx)
+        capi.check(lib.hlbg_halo_check(ctx), ctx)
+
+    def step(self, n: int = 1) -> None:
+        s = self.s
+        for _ in range(n):
+            s.StreamAndCollide(0, s.n_sites)
+            self.exchange()
+            s.PostStep(0, s.n_sites)
+            s.SwapOldAndNew()

@@ -8,7 +8,8 @@ distributions (hlbg_halo_unpack_device); then PostStep and the swap on every
 rank.  The host orders the phases (every wait is a stream synchronisation on the
 host; no kernel waits on another).  The owned sites then equal the single-context
 update bit for bit in FP64, FP32-deviation and FP16 storage: the exchange moves
-stored values, so it is exact in every form.
+stored values, so it is exact in every form.  The same holds with the library's
+exchange (halo.HaloExchange) run by two processes over gloo.
 """
 import ctypes as C
 
@@ -135,3 +136,88 @@ def test_halo_offsets_outside_the_arrays_are_reported():
     assert b"offset outside" in lib.hlbg_last_error(r.s.ctx)
     assert lib.hlbg_halo_check(r.s.ctx) == capi.HLBG_OK  # the flag is cleared
     assert np.array_equal(r.s.GetFNew(), before)
+
+
+# ---- the exchange between processes --------------------------------------------
+
+def _free_port():
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _process_rank(rank, world, port, precision, steps, out):
+    import os
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        _process_rank_body(rank, world, precision, steps, out)
+    except Exception:
+        import traceback
+        out.put((rank, "error", traceback.format_exc()))
+        raise
+    finally:
+        dist.destroy_process_group()
+
+
+def _process_rank_body(rank, world, precision, steps, out):
+    import torch.distributed as dist
+    c = _bifurcation()
+    ranks = halo.partition(c.geometry.view, world)
+    h = halo.Halo(c.geometry.view, ranks, world, rank)
+    params = c.params
+    s = LBM(h.view, type(params)(**{**params.__dict__, "precision": precision}), c.inlets, c.outlets)
+    s.SetInitialConditions()
+    ex = halo.HaloExchange(s, h)
+    ex.step(steps)
+    coords = s.site_coords()
+    owned = {tuple(x) for x in h.block_coords[: h.n_owned].tolist()}
+    mine = np.array([tuple(x) in owned for x in (coords // 8).tolist()])
+    out.put((rank, coords[mine].copy(), s.GetFOld()[mine].copy(), s.GetFNew()[mine].copy(),
+             sum(len(e.send) for e in h.exchanges)))
+    dist.barrier()
+    s.close()
+
+
+@pytest.mark.parametrize("precision", [capi.FP64, capi.FP32DEV])
+def test_processes_exchanging_over_gloo_equal_single_context(precision):
+    """halo.HaloExchange in two processes that share this GPU, one context each: the
+    device pack, the transport (gloo, staged through host memory; every wait is on
+    the host, between kernels), the device unpack.  The owned sites equal the
+    single-context update bit for bit after 30 steps."""
+    import torch.multiprocessing as mp
+    world, steps = 2, 30
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_process_rank, args=(r, world, port, precision, steps, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    parts = []
+    for _ in range(world):
+        x = q.get(timeout=300)
+        if isinstance(x[1], str):  # a rank failed: the other one may wait for it forever
+            for p in procs:
+                p.terminate()
+            pytest.fail(x[2])
+        parts.append(x)
+    for p in procs:
+        p.join(timeout=120)
+    assert all(p.exitcode == 0 for p in procs)
+    c = _bifurcation()
+    one = c.solver(precision)
+    one.SetInitialConditions()
+    one.DoTimeStep(steps)
+    index = {tuple(x): i for i, x in enumerate(one.site_coords().tolist())}
+    f_old, f_new = one.GetFOld(), one.GetFNew()
+    seen = np.zeros(one.n_sites, dtype=int)
+    for _, coords, fo, fn, sent in parts:
+        idx = np.array([index[tuple(x)] for x in coords.tolist()])
+        seen[idx] += 1
+        assert np.array_equal(fo, f_old[idx]) and np.array_equal(fn, f_new[idx])
+        assert sent > 0
+    assert np.all(seen == 1)

@@ -7,8 +7,8 @@
    site; edge blocks are exactly the owned blocks that stream into ghost blocks.
 3. The exchange, on gloo ranks (world size 2 and 4): each rank runs the oracle on
    its local geometry (owned + ghost blocks), sends the distributions its sites
-   streamed into ghost sites, scatters what it receives, then runs PostStep and
-   swaps -- the order of lb::LBM (Code/lb/lb.hpp:176-309) around
+   streamed into ghost sites (the library's transport, halo.exchange_buffers),
+   scatters what it receives, then runs PostStep and swaps -- the order of lb::LBM (Code/lb/lb.hpp:176-309) around
    FieldData::SendAndReceive / CopyReceived (Code/geometry/FieldData.cc:27-49).
    After every step the owned sites equal the single-rank run bit for bit.
 This is the host logic of a multi-GPU update; no GPU takes part.
@@ -159,16 +159,11 @@ def _rank_worker(rank, world, port, kind, steps, out):
         plans = [(ex.peer, _flat(h, ex.send, index), _flat(h, ex.recv, index)) for ex in h.exchanges]
         for _ in range(steps):
             o.stream_and_collide(0, o.n)
-            reqs, bufs = [], []
-            for peer, si, ri in plans:
-                reqs.append(dist.isend(torch.from_numpy(o.f_new[si].copy()), peer))
-                buf = torch.empty(len(ri), dtype=torch.float64)
-                reqs.append(dist.irecv(buf, peer))
-                bufs.append((ri, buf))
-            for r in reqs:
-                r.wait()
-            for ri, buf in bufs:
-                o.f_new[ri] = buf.numpy()
+            send = {peer: torch.from_numpy(o.f_new[si].copy()) for peer, si, _ in plans}
+            recv = {peer: torch.empty(len(ri), dtype=torch.float64) for peer, _, ri in plans}
+            halo.exchange_buffers(send, recv)  # the library's transport
+            for peer, _, ri in plans:
+                o.f_new[ri] = recv[peer].numpy()
             o.post_step(0, o.n)
             o.swap()
         # owned sites, keyed by coordinates
